@@ -1,0 +1,377 @@
+"""Benchmark: exact 2^24 x 2^24-limb multiplication on GB300.
+
+One step is one product of two 2^24-limb operands (uniform seeded 64-bit
+limbs, the balanced-sweep configuration the headline metric is quoted on):
+transform length 2^25, three 63-bit primes.  The metric is output limbs per
+second, (na + nb) / seconds per product, summed over ranks.
+
+  value   device-resident operands, hg_mul_device on the torch stream, timed
+          with CUDA events (operands 256 MiB + workspace 1.6 GB: larger than
+          L2, so no explicit flush).
+  e2e     the same product through the host C-ABI entry point hg_mul from
+          pinned host buffers, host->device and device->host copies inside
+          the timed region (wall clock around synchronous calls).
+  roofline  the kernel class with the most device time, its algorithmic
+          bytes over its event-timed duration, against the measured HBM copy
+          bandwidth.
+  cpu_baseline  the oracle (a C restatement of the reference's algorithm,
+          per-modulus threads like its with-parallel-work) timed on this
+          host on one full product.
+
+`--impl reference` times that CPU restatement instead (the reference itself
+is Common Lisp and cannot run here).  With --gpus N under torchrun each rank
+runs an independent replica; value is the sum over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "64-bit limbs multiplied/s at 2^24"
+UNIT = "limbs/s"
+LOG_SIZE = 24
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel_class: str):
+    """Per-launch DRAM bytes of a kernel class from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 3 and parts[0] == "dram_bytes_per_launch" and parts[1] == kernel_class:
+                    return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _cpu_info():
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return os.cpu_count() or 1, model
+
+
+def cpu_product_rate(log_size: int, threads: int) -> tuple[float, float]:
+    """One product of two 2^log_size-limb operands on the oracle; (limbs/s, s)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    from hypergeometrica_gb300 import workloads as W
+
+    n = 1 << log_size
+    x, y = W.limbs(1, n), W.limbs(2, n)
+    O.set_threads(threads)
+    t = time.perf_counter()
+    O.mpz_mul_ntt(x, y)
+    dt = time.perf_counter() - t
+    return 2 * n / dt, dt
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    cores, model = _cpu_info()
+    threads = min(6, cores)  # 2k forward tasks of with-parallel-work (k = 3 primes)
+    full = 1 << LOG_SIZE
+    # Size each step so that warm-up + timed steps stay within about 3 minutes.
+    rate20, t20 = cpu_product_rate(20, threads)
+    est_full = t20 * (full / (1 << 20)) * (25 / 21)
+    budget = 180.0 / max(1, args.steps + args.warmup)
+    log_s = LOG_SIZE
+    while log_s > 16 and est_full * (2 ** (log_s - LOG_SIZE)) > budget:
+        log_s -= 1
+    for _ in range(args.warmup):
+        cpu_product_rate(log_s, threads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_product_rate(log_s, threads)
+        times.append(dt)
+    total = sum(times)
+    n_out = 2 * (1 << log_s)
+    value = n_out * args.steps / total
+    sample = (f"one {1 << log_s}x{1 << log_s}-limb product per step" +
+              ("" if log_s == LOG_SIZE else f" (the {full}x{full} workload scaled down to fit the time budget)"))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (SplitMix64 seeds 1, 2)",
+        "config": {"workload": f"mul {full}x{full} limbs, transform 2^{LOG_SIZE + 1}, 3 primes",
+                   "dist": "uniform", "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "cpu": model, "host_cores": cores},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _residue_ok(out_u64, x_u64, y_u64) -> bool:
+    """out == x*y modulo the prime 2^31 - 1 (an O(n) sanity check)."""
+    import numpy as np
+
+    q = 2147483647
+    base = (1 << 64) % q
+
+    def full(a):
+        n = len(a)
+        blk = 4096
+        lo = np.empty(blk, dtype=np.uint64)
+        v = 1
+        for i in range(blk):
+            lo[i] = v
+            v = v * base % q
+        nb = (n + blk - 1) // blk
+        hi = np.empty(nb, dtype=np.uint64)
+        w = 1
+        for i in range(nb):
+            hi[i] = w
+            w = w * v % q
+        pw = np.tile(lo, nb)[:n] * np.repeat(hi, blk)[:n] % np.uint64(q)
+        return int(((a % np.uint64(q)) * pw % np.uint64(q)).sum(dtype=np.uint64) % np.uint64(q))
+
+    return full(out_u64) == full(x_u64) * full(y_u64) % q
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    from hypergeometrica_gb300 import build as B
+
+    if rank == 0 or ws == 1:
+        B.build()
+    if dist:
+        dist.barrier()
+    import hypergeometrica_gb300 as H
+    from hypergeometrica_gb300 import _lib
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import workloads as W
+
+    H.init(local)
+    na = nb = 1 << args.log_size
+    x = W.limbs(1 + 1000 * rank, na)
+    y = W.limbs(2 + 1000 * rank, nb)
+    tx = torch.from_numpy(x.view(np.int64)).cuda()
+    ty = torch.from_numpy(y.view(np.int64)).cuda()
+    out = torch.empty(na + nb, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        D.mul(tx, ty, out, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    D.sync(stream)
+    ok = _residue_ok(out.cpu().numpy().view(np.uint64), x, y)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    _lib.profile_read()  # reset counters
+    _lib.profile_enable(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    _lib.profile_enable(False)
+    prof = _lib.profile_read()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    D.sync(stream)
+
+    # End to end through the host entry point, pinned host buffers.
+    hx = torch.from_numpy(x.view(np.int64)).pin_memory()
+    hy = torch.from_numpy(y.view(np.int64)).pin_memory()
+    hout = torch.empty(na + nb, dtype=torch.int64).pin_memory()
+    lib = _lib.load()
+    rc = lib.hg_mul(hx.data_ptr(), na, hy.data_ptr(), nb, hout.data_ptr(), na + nb)  # warm the staging buffers
+    _lib.check(rc)
+    e2e_steps = max(3, min(args.steps, 20))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _lib.check(lib.hg_mul(hx.data_ptr(), na, hy.data_ptr(), nb, hout.data_ptr(), na + nb))
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    clocks = sampler.stop()
+    ok = ok and bool(np.array_equal(hout.numpy().view(np.uint64), out.cpu().numpy().view(np.uint64)))
+
+    n_out = na + nb
+    value = ws * n_out * args.steps / (ms / 1000.0)
+    e2e_value = ws * n_out * e2e_steps / e2e_s
+    launches = sum(v["launches"] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    peak, peak_kind = _peaks()
+    d = prof[dom]
+    achieved = (d["bytes"] / d["launches"]) / (d["ms"] / d["launches"] / 1000.0) / 1e9 if d["ms"] > 0 else 0.0
+    N = 1 << (args.log_size + 1)
+    b_mul = 16 * n_out + 192 * N  # minimum-pass algorithmic bytes of one product
+    prod_gbs = b_mul / (ms / args.steps / 1000.0) / 1e9
+    traffic = _traffic(dom)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (SplitMix64 limbs, seeds 1, 2 per rank)",
+        "config": {"workload": f"mul {na}x{nb} limbs, transform 2^{args.log_size + 1}, 3 primes",
+                   "dist": "uniform", "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "operands and workspace larger than L2; no flush"},
+        "correct": ok,
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (na + nb),
+                "d2h_bytes_per_step": 8 * n_out, "api": "hg_mul (host pointers, pinned)", "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_per_launch": d["bytes"] / max(1, d["launches"]),
+                     "launches": d["launches"], "ms_per_launch": d["ms"] / max(1, d["launches"])},
+        "roofline_product": {"algorithmic_bytes": b_mul, "achieved": prod_gbs, "frac": prod_gbs / peak,
+                             "unit": "GB/s", "formula": "16(na+nb) + 192 N"},
+        "kernels": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof.items() if v["launches"]},
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"],
+                   "samples": clocks["samples"]},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cores, model = _cpu_info()
+        threads = min(6, cores)
+        rate, dt = cpu_product_rate(args.log_size, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"one {na}x{nb}-limb product ({dt:.1f} s)", "cpu": model,
+                                "host_cores": cores}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--log-size", type=int, default=LOG_SIZE, help="log2 limbs per operand (default 24)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+"""ctypes binding of libhg_gb300.so (the C ABI in include/hypergeometrica_gb300.h).
+
+The library is the only compute path: if it is missing or fails to load,
+every call raises HGError.  There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libhg_gb300.so")
+HEADER = os.path.join(ROOT, "include", "hypergeometrica_gb300.h")
+
+HG_OK = 0
+HG_ERR_ARG = -1
+HG_ERR_MODULI = -2
+HG_ERR_OOM = -3
+HG_ERR_CUDA = -4
+HG_ERR_INCONSISTENT = -5
+HG_ERR_TIMEOUT = -6
+HG_ERR_NOT_INIT = -7
+
+ERROR_NAMES = {
+    HG_ERR_ARG: "HG_ERR_ARG",
+    HG_ERR_MODULI: "HG_ERR_MODULI",
+    HG_ERR_OOM: "HG_ERR_OOM",
+    HG_ERR_CUDA: "HG_ERR_CUDA",
+    HG_ERR_INCONSISTENT: "HG_ERR_INCONSISTENT",
+    HG_ERR_TIMEOUT: "HG_ERR_TIMEOUT",
+    HG_ERR_NOT_INIT: "HG_ERR_NOT_INIT",
+}
+
+
+class HGError(RuntimeError):
+    """A failed library call (the reference signals a CL error instead)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_sz = ctypes.c_size_t
+_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "hg_init": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int]),
+    "hg_shutdown": (ctypes.c_int, []),
+    "hg_last_error": (ctypes.c_int, [ctypes.c_char_p, _sz]),
+    "hg_scheme_moduli": (ctypes.c_int, [_u64p, ctypes.c_int]),
+    "hg_ntt_length": (_sz, [_sz, _sz]),
+    "hg_mul": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
+    "hg_sqr": (ctypes.c_int, [_vp, _sz, _vp, _sz]),
+    "hg_mul_schoolboy": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
+    "hg_mul_digit": (ctypes.c_int, [_vp, _sz, ctypes.c_uint64, _vp, _sz]),
+    "hg_mpz_mul": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp, _sz, ctypes.c_int, ctypes.c_int, _sz, _vp, _sz,
+                                  ctypes.POINTER(_sz), ctypes.POINTER(ctypes.c_int)]),
+    "hg_mul_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
+    "hg_sqr_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp]),
+    "hg_mul_schoolboy_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
+    "hg_sync": (ctypes.c_int, [_vp]),
+    "hg_ntt_forward_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
+    "hg_ntt_reverse_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
+    "hg_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "hg_profile_read": (ctypes.c_int, [_u64p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int]),
+}
+
+KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "pointwise", "carry", "small", "other"]
+
+
+def profile_enable(on: bool) -> None:
+    check(load().hg_profile_enable(1 if on else 0))
+
+
+def profile_read() -> dict:
+    """Per kernel class: launches, device ms (while recording) and algorithmic
+    bytes since the last read."""
+    n = len(KERNEL_CLASSES)
+    la = (ctypes.c_uint64 * n)()
+    ms = (ctypes.c_double * n)()
+    by = (ctypes.c_double * n)()
+    check(load().hg_profile_read(la, ms, by, n))
+    return {k: {"launches": int(la[i]), "ms": float(ms[i]), "bytes": float(by[i])}
+            for i, k in enumerate(KERNEL_CLASSES)}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def header_symbols(path: str = HEADER) -> list[str]:
+    """Function names declared in the public header."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    return re.findall(r"\b(hg_[a-z0-9_]+)\s*\(", text)
+
+
+def load() -> ctypes.CDLL:
+    """Load the library (once).  Raises HGError when it is not built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise HGError(HG_ERR_NOT_INIT, f"{LIB_PATH} is not built; run `python -m hypergeometrica_gb300.build`")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(512)
+    load().hg_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int) -> None:
+    if rc != HG_OK:
+        raise HGError(rc, last_error())

@@ -1,0 +1,770 @@
+// hg_api.cu -- host driver behind the C ABI (include/hypergeometrica_gb300.h).
+//
+// Owns the library context: the scheme (moduli and generators, rebuilt here
+// exactly as make-modular-scheme / default-moduli build them,
+// src/moduli.lisp:173-191, 257-353), the device twiddle tables, a grow-only
+// device workspace, the carry-scan state and the device error word.  Plans
+// the NTT passes for a transform length and enqueues the kernels of one
+// product: forward passes (the first reads the limbs and reduces them),
+// pointwise product, inverse passes, reconstruction + carry.
+#include <cstdarg>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hg_internal.h"
+#include "hypergeometrica_gb300.h"
+
+namespace hg {
+namespace {
+
+using u128 = unsigned __int128;
+
+// ---- host modular arithmetic -------------------------------------------
+uint64_t mulmod_h(uint64_t a, uint64_t b, uint64_t m) { return static_cast<uint64_t>((u128)a * b % m); }
+uint64_t powmod_h(uint64_t a, uint64_t e, uint64_t m) {
+  uint64_t r = 1 % m;
+  a %= m;
+  while (e) {
+    if (e & 1) r = mulmod_h(r, a, m);
+    a = mulmod_h(a, a, m);
+    e >>= 1;
+  }
+  return r;
+}
+uint64_t invmod_h(uint64_t x, uint64_t m) { return powmod_h(x % m, m - 2, m); }  // m prime
+uint64_t mont_h(uint64_t x, uint64_t m) { return static_cast<uint64_t>(((u128)(x % m) << 64) % m); }
+
+bool isprime_h(uint64_t n) {
+  if (n < 2) return false;
+  static const uint64_t bases[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+  for (uint64_t b : bases)
+    if (n % b == 0) return n == b;
+  uint64_t d = n - 1;
+  int s = 0;
+  while (!(d & 1)) {
+    d >>= 1;
+    ++s;
+  }
+  for (uint64_t b : bases) {
+    uint64_t x = powmod_h(b, d, n);
+    if (x == 1 || x == n - 1) continue;
+    bool comp = true;
+    for (int r = 1; r < s && comp; ++r) {
+      x = mulmod_h(x, x, n);
+      if (x == n - 1) comp = false;
+    }
+    if (comp) return false;
+  }
+  return true;
+}
+
+// find-finite-field-generator (src/moduli.lisp:173-179): smallest prime g
+// with g^((m-1)/f) != 1 for each prime factor f of m - 1.
+uint64_t generator_h(uint64_t m) {
+  std::vector<uint64_t> f;
+  uint64_t n = m - 1;
+  for (uint64_t q = 2; q * q <= n; ++q)
+    if (n % q == 0) {
+      f.push_back(q);
+      while (n % q == 0) n /= q;
+    }
+  if (n > 1) f.push_back(n);
+  for (uint64_t g = 2;; ++g) {
+    if (!isprime_h(g)) continue;
+    bool ok = true;
+    for (uint64_t q : f)
+      if (powmod_h(g, (m - 1) / q, m) == 1) ok = false;
+    if (ok) return g;
+  }
+}
+
+// default-moduli (src/moduli.lisp:257-264): primes c*2^55 + 1 of integer
+// length 63, largest first.
+std::vector<uint64_t> default_moduli_h() {
+  std::vector<uint64_t> v;
+  for (uint64_t c = 255; c >= 128; --c) {
+    const uint64_t p = (c << kShift) + 1;
+    if (isprime_h(p)) v.push_back(p);
+  }
+  return v;
+}
+
+// ---- context -----------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  uint64_t *u64() const { return static_cast<uint64_t *>(p); }
+};
+
+struct Context {
+  bool ready = false;
+  int device = 0;
+  uint64_t moduli[kPrimes] = {};
+  uint64_t gens[kPrimes] = {};
+  PrimeConst pc[kPrimes] = {};
+  NttTables tb[kPrimes] = {};
+  DevBuf tables;
+  cudaStream_t stream = nullptr;
+  DevBuf A, B, X, Y, OUT, flags;
+  DevBuf misc;  // [0] ticket (u64), [1] error word (int)
+  unsigned long long ticket_count = 0;
+  uint32_t epoch = 0;
+  cudaEvent_t ws_done = nullptr;
+  bool ws_pending = false;
+  std::recursive_mutex mu;
+};
+
+Context g_ctx;
+thread_local std::string t_err;
+
+// ---- instrumentation: launch counters and optional event timing ---------
+struct ProfRecord {
+  int cls;
+  cudaEvent_t b, e;
+};
+struct Profile {
+  std::mutex mu;
+  bool on = false;
+  uint64_t launches[HG_KC_COUNT] = {};
+  double bytes[HG_KC_COUNT] = {};
+  std::vector<ProfRecord> recs;
+};
+Profile g_prof;
+
+// Counts one kernel launch of class `cls` moving `bytes` algorithmic bytes,
+// bracketed by a CUDA event pair on `st` while recording is on.
+class ProfScope {
+ public:
+  ProfScope(int cls, cudaStream_t st, double bytes) : cls_(cls), st_(st) {
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    g_prof.launches[cls]++;
+    g_prof.bytes[cls] += bytes;
+    if (g_prof.on && cudaEventCreate(&b_) == cudaSuccess) cudaEventRecord(b_, st_);
+  }
+  ~ProfScope() {
+    if (!b_) return;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) == cudaSuccess) {
+      cudaEventRecord(e, st_);
+      std::lock_guard<std::mutex> lk(g_prof.mu);
+      g_prof.recs.push_back({cls_, b_, e});
+    } else {
+      cudaEventDestroy(b_);
+    }
+  }
+
+ private:
+  int cls_;
+  cudaStream_t st_;
+  cudaEvent_t b_ = nullptr;
+};
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  if (e == cudaErrorMemoryAllocation) return fail(HG_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(HG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define HG_CUDA(call, what)                   \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+constexpr size_t kSubWords = 2048;
+constexpr size_t kLevelWords = size_t(1) << kTwLevelBits;
+constexpr size_t kPrimeTableWords = 2 * kSubWords + 4 * kLevelWords;
+
+int init_locked(const uint64_t *moduli, int k, int device) {
+  Context &c = g_ctx;
+  std::vector<uint64_t> dm = default_moduli_h();
+  if (dm.size() != kPrimes) return fail(HG_ERR_NOT_INIT, "expected %d default moduli, found %zu", kPrimes, dm.size());
+  if (moduli && k > 0) {
+    std::vector<uint64_t> given(moduli, moduli + k);
+    std::sort(given.begin(), given.end(), [](uint64_t a, uint64_t b) { return a > b; });
+    if (given != dm)
+      return fail(HG_ERR_NOT_INIT, "moduli differ from the scheme this library implements (default-moduli)");
+  }
+  if (c.ready) {
+    if (device >= 0 && device != c.device)
+      return fail(HG_ERR_ARG, "library already initialised on device %d", c.device);
+    return HG_OK;
+  }
+  if (device >= 0) HG_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  HG_CUDA(cudaGetDevice(&c.device), "cudaGetDevice");
+  std::vector<uint64_t> host(kPrimeTableWords * kPrimes);
+  for (int i = 0; i < kPrimes; ++i) {
+    const uint64_t p = dm[i];
+    c.moduli[i] = p;
+    c.pc[i] = PrimeConst{p, static_cast<uint32_t>(p >> kShift), 0};
+    c.gens[i] = generator_h(p);
+    const uint64_t w30 = powmod_h(c.gens[i], (p - 1) >> kLogNmax, p);
+    const uint64_t w30i = invmod_h(w30, p);
+    const uint64_t w4096 = powmod_h(w30, uint64_t(1) << (kLogNmax - kTileBits), p);
+    const uint64_t w4096i = invmod_h(w4096, p);
+    uint64_t *t = host.data() + i * kPrimeTableWords;
+    uint64_t *sub_f = t, *sub_i = t + kSubWords, *hi_f = t + 2 * kSubWords, *lo_f = hi_f + kLevelWords,
+             *hi_i = lo_f + kLevelWords, *lo_i = hi_i + kLevelWords;
+    uint64_t a = 1, b = 1;
+    for (size_t e = 0; e < kSubWords; ++e) {
+      sub_f[e] = mont_h(a, p);
+      sub_i[e] = mont_h(b, p);
+      a = mulmod_h(a, w4096, p);
+      b = mulmod_h(b, w4096i, p);
+    }
+    const uint64_t step_f = powmod_h(w30, kLevelWords, p), step_i = powmod_h(w30i, kLevelWords, p);
+    uint64_t lf = 1, li = 1, hf = 1, hi = 1;
+    for (size_t e = 0; e < kLevelWords; ++e) {
+      lo_f[e] = mont_h(lf, p);
+      lo_i[e] = mont_h(li, p);
+      hi_f[e] = mont_h(hf, p);
+      hi_i[e] = mont_h(hi, p);
+      lf = mulmod_h(lf, w30, p);
+      li = mulmod_h(li, w30i, p);
+      hf = mulmod_h(hf, step_f, p);
+      hi = mulmod_h(hi, step_i, p);
+    }
+  }
+  HG_CUDA(c.tables.ensure(host.size() * sizeof(uint64_t)), "table allocation");
+  HG_CUDA(cudaMemcpy(c.tables.p, host.data(), host.size() * sizeof(uint64_t), cudaMemcpyHostToDevice), "table upload");
+  for (int i = 0; i < kPrimes; ++i) {
+    const uint64_t *t = c.tables.u64() + i * kPrimeTableWords;
+    c.tb[i].sub_fwd = t;
+    c.tb[i].sub_inv = t + kSubWords;
+    c.tb[i].hi_fwd = t + 2 * kSubWords;
+    c.tb[i].lo_fwd = c.tb[i].hi_fwd + kLevelWords;
+    c.tb[i].hi_inv = c.tb[i].lo_fwd + kLevelWords;
+    c.tb[i].lo_inv = c.tb[i].hi_inv + kLevelWords;
+  }
+  HG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream creation");
+  HG_CUDA(cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming), "event creation");
+  HG_CUDA(c.misc.ensure(64), "scan state allocation");
+  HG_CUDA(cudaMemset(c.misc.p, 0, 64), "scan state init");
+  c.ready = true;
+  return HG_OK;
+}
+
+int ensure_init() {
+  if (g_ctx.ready) return HG_OK;
+  return init_locked(nullptr, 0, -1);
+}
+
+int ilog2_ceil(uint64_t n) {
+  int l = 0;
+  while ((uint64_t(1) << l) < n) ++l;
+  return l;
+}
+
+uint64_t trimmed(const uint64_t *x, uint64_t n) {
+  while (n > 0 && x[n - 1] == 0) --n;
+  return n;
+}
+
+struct PassPlan {
+  int logR, logS, logT;
+};
+
+// Passes for N = 2^L: strided passes of at most 8 rows-bits (tiles of 4096
+// residues with >= 16 columns, i.e. >= 128-byte row segments), then one
+// contiguous pass over 4096-residue blocks.
+std::vector<PassPlan> plan_passes(int L) {
+  std::vector<PassPlan> v;
+  if (L <= kTileBits) {
+    v.push_back({L, 0, L});
+    return v;
+  }
+  const int rem = L - kTileBits;
+  const int k = (rem + 7) / 8;
+  int logS = L;
+  for (int i = 0; i < k; ++i) {
+    const int part = rem / k + (i < rem % k ? 1 : 0);
+    logS -= part;
+    v.push_back({part, logS, kTileBits});
+  }
+  v.push_back({kTileBits, 0, kTileBits});
+  return v;
+}
+
+PassArgs base_args(int L, int nops) {
+  PassArgs a{};
+  a.nops = nops;
+  a.logN = L;
+  a.prime_lo = 0;
+  a.nprimes = kPrimes;
+  a.prime_stride = uint64_t(1) << L;
+  for (int i = 0; i < kPrimes; ++i) {
+    a.pc[i] = g_ctx.pc[i];
+    a.tb[i] = g_ctx.tb[i];
+  }
+  return a;
+}
+
+cudaError_t run_passes(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
+  const int np = static_cast<int>(plan.size());
+  for (int s = 0; s < np; ++s) {
+    const PassPlan &pp = plan[inverse ? np - 1 - s : s];
+    a.logR = pp.logR;
+    a.logS = pp.logS;
+    a.logT = pp.logT;
+    a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
+    // Algorithmic bytes: each residue read and written once; the first
+    // forward pass reads limbs instead of residues.
+    const double words = static_cast<double>(a.nprimes) * static_cast<double>(uint64_t(1) << a.logN);
+    double bytes = 0;
+    for (int op = 0; op < a.nops; ++op)
+      bytes += 8.0 * words + (a.limbs[op] ? 8.0 * static_cast<double>(a.nlimbs[op]) : 8.0 * words);
+    cudaError_t e;
+    {
+      ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, bytes);
+      e = launch_ntt_pass(a, inverse, st);
+    }
+    if (e != cudaSuccess) return e;
+    a.limbs[0] = a.limbs[1] = nullptr;  // only the first forward pass reads limbs
+  }
+  return cudaSuccess;
+}
+
+CrtConst crt_const(int L) {
+  CrtConst k{};
+  const uint64_t p0 = g_ctx.moduli[0], p1 = g_ctx.moduli[1], p2 = g_ctx.moduli[2];
+  for (int i = 0; i < kPrimes; ++i) k.pc[i] = g_ctx.pc[i];
+  const uint64_t N = uint64_t(1) << L;
+  const uint64_t n0 = invmod_h(N % p0, p0), n1 = invmod_h(N % p1, p1), n2 = invmod_h(N % p2, p2);
+  const uint64_t R0 = mont_h(1, p0), R1 = mont_h(1, p1), R2 = mont_h(1, p2);  // 2^64 mod p
+  const uint64_t inv01 = invmod_h(p0 % p1, p1);
+  const uint64_t inv012 = invmod_h(mulmod_h(p0 % p2, p1 % p2, p2), p2);
+  k.k0 = mont_h(mulmod_h(n0, R0, p0), p0);
+  k.k1a = mont_h(mulmod_h(mulmod_h(n1, R1, p1), inv01, p1), p1);
+  k.k1b = mont_h(inv01, p1);
+  k.k2a = mont_h(mulmod_h(mulmod_h(n2, R2, p2), inv012, p2), p2);
+  k.k2b = mont_h(inv012, p2);
+  k.k2c = mont_h(mulmod_h(p0 % p2, inv012, p2), p2);
+  const u128 p01 = (u128)p0 * p1;
+  k.p01_lo = static_cast<uint64_t>(p01);
+  k.p01_hi = static_cast<uint64_t>(p01 >> 64);
+  return k;
+}
+
+// Serialise use of the shared workspace across streams.
+cudaError_t ws_acquire(cudaStream_t st) {
+  if (g_ctx.ws_pending) return cudaStreamWaitEvent(st, g_ctx.ws_done, 0);
+  return cudaSuccess;
+}
+cudaError_t ws_release(cudaStream_t st) {
+  g_ctx.ws_pending = true;
+  return cudaEventRecord(g_ctx.ws_done, st);
+}
+
+int scan_state(uint64_t tiles, ScanState *ss) {
+  Context &c = g_ctx;
+  const size_t need = (tiles + 1) * sizeof(unsigned long long);
+  if (need > c.flags.bytes) {
+    HG_CUDA(cudaDeviceSynchronize(), "sync before flag growth");
+    HG_CUDA(c.flags.ensure(need * 2), "flag allocation");
+    HG_CUDA(cudaMemset(c.flags.p, 0, c.flags.bytes), "flag init");
+  }
+  if (++c.epoch == 0) c.epoch = 1;
+  ss->ticket = static_cast<unsigned long long *>(c.misc.p);
+  ss->ticket_base = c.ticket_count;
+  ss->flags = static_cast<unsigned long long *>(c.flags.p);
+  ss->epoch = c.epoch;
+  ss->err = reinterpret_cast<int *>(static_cast<char *>(c.misc.p) + 8);
+  c.ticket_count += tiles;
+  return HG_OK;
+}
+
+int check_len(int L) {
+  if (L > kLogNmax) return fail(HG_ERR_ARG, "transform length 2^%d exceeds the supported 2^%d", L, kLogNmax);
+  return HG_OK;
+}
+
+// |x| * |y| (or |x|^2 when y == nullptr) into out[0, nout) on device memory.
+int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out, uint64_t nout,
+                       cudaStream_t st) {
+  Context &c = g_ctx;
+  const bool square = (y == nullptr);
+  if (square) ny = nx;
+  const uint64_t size = nx + ny;
+  if (!out || (nx && !x) || (!square && ny && !y)) return fail(HG_ERR_ARG, "null pointer");
+  if (nout < size) return fail(HG_ERR_ARG, "nout = %llu cannot hold the %llu-limb product", (unsigned long long)nout,
+                               (unsigned long long)size);
+  if (nx == 0 || ny == 0) {
+    HG_CUDA(cudaMemsetAsync(out, 0, nout * sizeof(uint64_t), st), "zero product");
+    return HG_OK;
+  }
+  const int L = ilog2_ceil(size);
+  int rc = check_len(L);
+  if (rc) return rc;
+  const uint64_t N = uint64_t(1) << L;
+  const size_t words = static_cast<size_t>(kPrimes) * N;
+  HG_CUDA(ws_acquire(st), "workspace ordering");
+  if (c.A.bytes < words * 8 || (!square && c.B.bytes < words * 8)) {
+    HG_CUDA(cudaDeviceSynchronize(), "sync before workspace growth");
+    HG_CUDA(c.A.ensure(words * 8), "workspace allocation");
+    if (!square) HG_CUDA(c.B.ensure(words * 8), "workspace allocation");
+  }
+  const std::vector<PassPlan> plan = plan_passes(L);
+  PassArgs a = base_args(L, square ? 1 : 2);
+  a.data[0] = c.A.u64();
+  a.data[1] = c.B.u64();
+  a.limbs[0] = x;
+  a.limbs[1] = y;
+  a.nlimbs[0] = nx;
+  a.nlimbs[1] = ny;
+  HG_CUDA(run_passes(a, plan, false, st), "forward transform");
+  {
+    ProfScope ps(HG_KC_POINTWISE, st, 8.0 * static_cast<double>(words) * (square ? 2 : 3));
+    HG_CUDA(launch_pointwise(c.A.u64(), square ? nullptr : c.B.u64(), L, c.pc, square, st), "pointwise product");
+  }
+  PassArgs inv = base_args(L, 1);
+  inv.data[0] = c.A.u64();
+  HG_CUDA(run_passes(inv, plan, true, st), "inverse transform");
+  if (nout > N) HG_CUDA(cudaMemsetAsync(out + N, 0, (nout - N) * sizeof(uint64_t), st), "zero tail");
+  ScanState ss;
+  const uint64_t nproc = nout < N ? nout : N;
+  rc = scan_state(carry_tiles(nproc), &ss);
+  if (rc) return rc;
+  uint64_t tiles = 0;
+  {
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(nproc));
+    HG_CUDA(launch_crt_carry(c.A.u64(), L, crt_const(L), out, nout, ss, st, &tiles), "reconstruction");
+  }
+  HG_CUDA(ws_release(st), "workspace ordering");
+  return HG_OK;
+}
+
+int small_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t d, uint64_t *out,
+                         uint64_t nout, cudaStream_t st) {
+  const uint64_t size = y ? nx + ny : nx + 1;
+  if (!out || (nx && !x)) return fail(HG_ERR_ARG, "null pointer");
+  if (y && nx < ny) return fail(HG_ERR_ARG, "schoolboy needs nx >= ny");
+  if (nout < size) return fail(HG_ERR_ARG, "nout = %llu cannot hold the %llu-limb product", (unsigned long long)nout,
+                               (unsigned long long)size);
+  if (nx == 0 || (y && ny == 0) || (!y && d == 0)) {
+    HG_CUDA(cudaMemsetAsync(out, 0, nout * sizeof(uint64_t), st), "zero product");
+    return HG_OK;
+  }
+  if (nout > size) HG_CUDA(cudaMemsetAsync(out + size, 0, (nout - size) * sizeof(uint64_t), st), "zero tail");
+  HG_CUDA(ws_acquire(st), "workspace ordering");
+  ScanState ss;
+  int rc = scan_state(carry_tiles(size), &ss);
+  if (rc) return rc;
+  uint64_t tiles = 0;
+  {
+    ProfScope ps(HG_KC_SMALL, st, 8.0 * static_cast<double>(nx + (y ? ny : 0) + size));
+    if (y)
+      HG_CUDA(launch_schoolboy_carry(x, nx, y, ny, out, size, ss, st, &tiles), "schoolboy product");
+    else
+      HG_CUDA(launch_digit_carry(x, nx, d, out, size, ss, st, &tiles), "digit product");
+  }
+  HG_CUDA(ws_release(st), "workspace ordering");
+  return HG_OK;
+}
+
+int read_device_error(cudaStream_t st) {
+  int err = 0;
+  int *d_err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
+  HG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st), "error word read");
+  HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
+  if (err) {
+    HG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st), "error word reset");
+    HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
+    if (err == kDevTimeout) return fail(HG_ERR_TIMEOUT, "a carry look-back wait ran out; results are invalid");
+    if (err == kDevCarryOverflow) return fail(HG_ERR_INCONSISTENT, "a carry left the top of the result storage");
+    return fail(HG_ERR_CUDA, "device error %d", err);
+  }
+  return HG_OK;
+}
+
+// Host-memory wrapper: stage operands, run, copy back, check.
+enum class Kind { Ntt, Square, Schoolboy, Digit };
+
+int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t d, uint64_t *out,
+                 size_t nout) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  Context &c = g_ctx;
+  if (!out || (nx && !x) || (ny && !y && (kind == Kind::Ntt || kind == Kind::Schoolboy)))
+    return fail(HG_ERR_ARG, "null pointer");
+  nx = trimmed(x, nx);
+  if (kind == Kind::Ntt || kind == Kind::Schoolboy) ny = trimmed(y, ny);
+  if (kind == Kind::Square) ny = nx;
+  if (kind == Kind::Digit) ny = 1;
+  const size_t size = nx + ny;
+  if (nout < size) return fail(HG_ERR_ARG, "nout = %zu cannot hold the %zu-limb product", nout, size);
+  if (kind == Kind::Schoolboy && nx < ny) return fail(HG_ERR_ARG, "schoolboy needs nx >= ny");
+  const bool zero = nx == 0 || ((kind == Kind::Ntt || kind == Kind::Schoolboy) && ny == 0) ||
+                    (kind == Kind::Digit && d == 0);
+  if (zero) {
+    memset(out, 0, nout * sizeof(uint64_t));
+    return HG_OK;
+  }
+  const size_t nd = size;  // limbs computed on the device; the rest are zero
+  cudaStream_t st = c.stream;
+  HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
+  HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
+  if (kind == Kind::Ntt || kind == Kind::Schoolboy) {
+    HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
+    HG_CUDA(cudaMemcpyAsync(c.Y.p, y, ny * 8, cudaMemcpyHostToDevice, st), "operand upload");
+  }
+  HG_CUDA(c.OUT.ensure(nd * 8), "result allocation");
+  switch (kind) {
+    case Kind::Ntt: rc = ntt_product_device(c.X.u64(), nx, c.Y.u64(), ny, c.OUT.u64(), nd, st); break;
+    case Kind::Square: rc = ntt_product_device(c.X.u64(), nx, nullptr, 0, c.OUT.u64(), nd, st); break;
+    case Kind::Schoolboy: rc = small_product_device(c.X.u64(), nx, c.Y.u64(), ny, 0, c.OUT.u64(), nd, st); break;
+    case Kind::Digit: rc = small_product_device(c.X.u64(), nx, nullptr, 0, d, c.OUT.u64(), nd, st); break;
+  }
+  if (rc) return rc;
+  HG_CUDA(cudaMemcpyAsync(out, c.OUT.p, nd * 8, cudaMemcpyDeviceToHost, st), "result download");
+  rc = read_device_error(st);
+  if (rc) return rc;
+  if (nout > nd) memset(out + nd, 0, (nout - nd) * sizeof(uint64_t));
+  return HG_OK;
+}
+
+int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!a) return fail(HG_ERR_ARG, "null pointer");
+  if (mod_num < 0 || mod_num >= kPrimes) return fail(HG_ERR_ARG, "modulus index %d out of range", mod_num);
+  if (n == 0 || (n & (n - 1))) return fail(HG_ERR_ARG, "length %zu is not a power of two", n);
+  if (n == 1) return HG_OK;
+  const int L = ilog2_ceil(n);
+  rc = check_len(L);
+  if (rc) return rc;
+  PassArgs pa = base_args(L, 1);
+  pa.data[0] = a;
+  pa.prime_lo = mod_num;
+  pa.nprimes = 1;
+  pa.prime_stride = 0;
+  HG_CUDA(run_passes(pa, plan_passes(L), inverse, st), "transform");
+  if (inverse) {
+    const uint64_t p = g_ctx.moduli[mod_num];
+    ProfScope ps(HG_KC_OTHER, st, 16.0 * static_cast<double>(n));
+    HG_CUDA(launch_scale(a, n, mont_h(invmod_h(n % p, p), p), g_ctx.pc[mod_num], st), "1/N scaling");
+  }
+  return HG_OK;
+}
+
+}  // namespace
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+int hg_init(const uint64_t *moduli, int k, int device) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  return init_locked(moduli, k, device);
+}
+
+int hg_shutdown(void) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  Context &c = g_ctx;
+  if (!c.ready) return HG_OK;
+  cudaDeviceSynchronize();
+  c.A.release();
+  c.B.release();
+  c.X.release();
+  c.Y.release();
+  c.OUT.release();
+  c.flags.release();
+  c.misc.release();
+  c.tables.release();
+  if (c.stream) cudaStreamDestroy(c.stream);
+  if (c.ws_done) cudaEventDestroy(c.ws_done);
+  c.stream = nullptr;
+  c.ws_done = nullptr;
+  c.ws_pending = false;
+  c.ready = false;
+  return HG_OK;
+}
+
+int hg_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return HG_ERR_ARG;
+  snprintf(buf, len, "%s", t_err.c_str());
+  return HG_OK;
+}
+
+int hg_scheme_moduli(uint64_t *out, int cap) {
+  std::vector<uint64_t> dm = default_moduli_h();
+  for (int i = 0; i < cap && i < static_cast<int>(dm.size()); ++i) out[i] = dm[i];
+  return static_cast<int>(dm.size());
+}
+
+size_t hg_ntt_length(size_t nx, size_t ny) {
+  const size_t s = nx + ny;
+  size_t r = 1;
+  while (r < s) r <<= 1;
+  return r;
+}
+
+int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout) {
+  return host_product(Kind::Ntt, x, nx, y, ny, 0, out, nout);
+}
+
+int hg_sqr(const uint64_t *x, size_t nx, uint64_t *out, size_t nout) {
+  return host_product(Kind::Square, x, nx, nullptr, 0, 0, out, nout);
+}
+
+int hg_mul_schoolboy(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout) {
+  return host_product(Kind::Schoolboy, x, nx, y, ny, 0, out, nout);
+}
+
+int hg_mul_digit(const uint64_t *x, size_t nx, uint64_t d, uint64_t *out, size_t nout) {
+  return host_product(Kind::Digit, x, nx, nullptr, 0, d, out, nout);
+}
+
+int hg_mpz_mul(const uint64_t *x, size_t nx, int sx, const uint64_t *y, size_t ny, int sy, int same_object,
+               size_t threshold, uint64_t *out, size_t nout, size_t *nres, int *sres) {
+  if (!nres || !sres || !out || (nx && !x) || (ny && !y)) return fail(HG_ERR_ARG, "null pointer");
+  nx = trimmed(x, nx);
+  ny = trimmed(y, ny);
+  if (nx < ny) {  // rotatef so that |x| >= |y| (src/multiply.lisp:15-16)
+    std::swap(x, y);
+    std::swap(nx, ny);
+    std::swap(sx, sy);
+  }
+  int rc = HG_OK;
+  int sign = sx * sy;
+  if (ny == 0) {  // (src/multiply.lisp:21-22)
+    *nres = 0;
+    *sres = 1;
+    return HG_OK;
+  }
+  if (ny == 1) {  // (src/multiply.lisp:23-36)
+    const uint64_t d = y[0];
+    if (d == 1) {
+      if (nout < nx) return fail(HG_ERR_ARG, "nout too small");
+      memmove(out, x, nx * sizeof(uint64_t));
+      sign = (sy == -1) ? -sx : sx;
+    } else {
+      rc = hg_mul_digit(x, nx, d, out, nout);
+    }
+  } else if (ny <= threshold) {  // (src/multiply.lisp:37-42)
+    rc = hg_mul_schoolboy(x, nx, y, ny, out, nout);
+  } else if (same_object) {  // (src/multiply.lisp:43-44)
+    rc = hg_sqr(x, nx, out, nout);
+    sign = 1;
+  } else {  // (src/multiply.lisp:48-49)
+    rc = hg_mul(x, nx, y, ny, out, nout);
+  }
+  if (rc) return rc;
+  *nres = trimmed(out, nout);
+  *sres = *nres ? sign : 1;
+  return HG_OK;
+}
+
+int hg_mul_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
+                  void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  return ntt_product_device(x, nx, y, ny, out, nout, static_cast<cudaStream_t>(stream));
+}
+
+int hg_sqr_device(const uint64_t *x, size_t nx, uint64_t *out, size_t nout, void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  return ntt_product_device(x, nx, nullptr, 0, out, nout, static_cast<cudaStream_t>(stream));
+}
+
+int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
+                            void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!y) return fail(HG_ERR_ARG, "null pointer");
+  return small_product_device(x, nx, y, ny, 0, out, nout, static_cast<cudaStream_t>(stream));
+}
+
+int hg_sync(void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!st) {
+    HG_CUDA(cudaDeviceSynchronize(), "device synchronise");
+    st = g_ctx.stream;
+  }
+  return read_device_error(st);
+}
+
+int hg_ntt_forward_device(uint64_t *a, size_t n, int mod_num, void *stream) {
+  return spectrum(a, n, mod_num, false, static_cast<cudaStream_t>(stream));
+}
+
+int hg_ntt_reverse_device(uint64_t *a, size_t n, int mod_num, void *stream) {
+  return spectrum(a, n, mod_num, true, static_cast<cudaStream_t>(stream));
+}
+
+int hg_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof.on = on != 0;
+  return HG_OK;
+}
+
+int hg_profile_read(uint64_t *launches, double *ms, double *bytes, int cap) {
+  std::vector<ProfRecord> recs;
+  uint64_t l[HG_KC_COUNT];
+  double b[HG_KC_COUNT];
+  {
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    recs.swap(g_prof.recs);
+    for (int i = 0; i < HG_KC_COUNT; ++i) {
+      l[i] = g_prof.launches[i];
+      b[i] = g_prof.bytes[i];
+      g_prof.launches[i] = 0;
+      g_prof.bytes[i] = 0;
+    }
+  }
+  double t[HG_KC_COUNT] = {};
+  int rc = HG_OK;
+  for (const ProfRecord &r : recs) {
+    float dt = 0;
+    if (cudaEventSynchronize(r.e) == cudaSuccess && cudaEventElapsedTime(&dt, r.b, r.e) == cudaSuccess)
+      t[r.cls] += dt;
+    else
+      rc = fail(HG_ERR_CUDA, "profiling event failed");
+    cudaEventDestroy(r.b);
+    cudaEventDestroy(r.e);
+  }
+  for (int i = 0; i < cap && i < HG_KC_COUNT; ++i) {
+    if (launches) launches[i] = l[i];
+    if (ms) ms[i] = t[i];
+    if (bytes) bytes[i] = b[i];
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// hg_common.cuh -- shared definitions of the GB300 multiplication library.
+//
+// Arithmetic is modulo the reference's three NTT primes (default-moduli,
+// src/moduli.lisp:257-264): p = c * 2^55 + 1 with c = 197, 174, 131.  That
+// shape makes Montgomery reduction with R = 2^64 cheap: p^-1 mod 2^64 is
+// 1 - c*2^55, and floor(m*p / 2^64) needs only a 64 x 8-bit product.  The
+// reference's Barrett (m*/fast, src/modular-arithmetic.lisp:167-202) and
+// Shoup (m*/fast2, :207-231) multiplications compute the same residues; only
+// the instruction sequence differs.  Data stays in normal form; twiddles are
+// stored in Montgomery form (w * 2^64 mod p), so mont_mul(x, w~) = x*w mod p.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hg {
+
+constexpr int kPrimes = 3;      // moduli in the scheme
+constexpr int kShift = 55;      // p = c * 2^kShift + 1
+constexpr int kLogNmax = 30;    // largest transform: 2^30 limbs
+constexpr int kTwLevelBits = 15;  // two-level twiddle tables: 2^15 entries per level
+constexpr int kTileBits = 12;   // in-CTA transform tile: 2^12 residues
+constexpr int kTileThreads = 256;
+constexpr int kPerThread = 16;  // residues held in registers per thread
+
+// Per-prime constants.
+struct PrimeConst {
+  uint64_t p;
+  uint32_t c;  // p = c * 2^55 + 1
+  uint32_t pad;
+};
+
+// Device error word codes (latched with atomicCAS; first error wins).
+enum DevErr : int {
+  kDevOk = 0,
+  kDevTimeout = 1,        // a look-back wait ran out of iterations
+  kDevCarryOverflow = 2,  // a carry left the top of the result
+  kDevTicket = 3,         // a carry-scan tile ticket fell outside its launch
+};
+
+__host__ __device__ __forceinline__ uint64_t add_mod(uint64_t a, uint64_t b, uint64_t p) {
+  uint64_t s = a + b;  // a, b < p < 2^63
+  return s >= p ? s - p : s;
+}
+
+__host__ __device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uint64_t p) {
+  uint64_t d = a - b;
+  return a < b ? d + p : d;
+}
+
+__device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __umul64hi(a, b); }
+
+// Montgomery product a * b * 2^-64 mod p, for any 64-bit a and b < p, with
+// p = c * 2^55 + 1.  Result is fully reduced in [0, p).
+__device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p, uint32_t c) {
+  const uint64_t lo = a * b;
+  const uint64_t hi = mul_hi64(a, b);  // < p because a < 2^64 and b < p
+  // m = lo * p^-1 mod 2^64 = lo - ((lo * c) mod 2^9) * 2^55
+  const uint32_t lo0 = static_cast<uint32_t>(lo);
+  const uint64_t m = lo - (static_cast<uint64_t>(lo0 * (c << 23)) << 32);
+  // floor(m * p / 2^64) = floor((m * c + floor(m / 2^55)) / 2^9)
+  const uint64_t t = static_cast<uint64_t>(static_cast<uint32_t>(m)) * c + (m >> kShift);
+  const uint64_t u = (m >> 32) * c + (t >> 32);
+  const uint64_t mph = (u << 23) | (static_cast<uint32_t>(t) >> 9);
+  const uint64_t r = hi - mph;  // low halves cancel exactly
+  return hi < mph ? r + p : r;
+}
+
+// x mod p for any 64-bit x (x < 4p because p > 2^62).
+__device__ __forceinline__ uint64_t reduce64(uint64_t x, uint64_t p) {
+  const uint64_t p2 = p << 1;
+  if (x >= p2) x -= p2;
+  return x >= p ? x - p : x;
+}
+
+// Carry-lookahead pair for the final carry scan: with carry-in c, a
+// position (or a run of positions) emits carry g | (p & c).
+struct GP {
+  uint32_t g, p;
+};
+// Compose: first `lo` (less significant run), then `hi`.
+__host__ __device__ __forceinline__ GP gp_compose(GP lo, GP hi) {
+  return GP{hi.g | (hi.p & lo.g), hi.p & lo.p};
+}
+
+}  // namespace hg

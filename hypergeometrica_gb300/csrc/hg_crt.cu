@@ -1,0 +1,279 @@
+// hg_crt.cu -- coefficient reconstruction and carry propagation.
+//
+// The reference rebuilds each convolution coefficient as a bignum
+// sum_j f_j r_j mod M (f_j = (M/m_j) * ((M/m_j)^-1 mod m_j)) and adds it at
+// limb i with a recursive carry ripple (src/ntt-multiply.lisp:10-51,
+// 242-253).  The value is the unique residue mod M = m0 m1 m2, so any exact
+// reconstruction gives the same limbs.  Here Garner's mixed radix
+// (src/modular-arithmetic.lisp:235-267) produces each coefficient as three
+// limbs V_i = y0 + p0 t1 + p0 p1 t2, the overlap-add sum_i V_i 2^(64 i) is
+// formed per position, and carries are resolved by a carry-lookahead scan:
+// within a CTA by warp shuffles, across CTAs by decoupled look-back on
+// per-tile flags.  Every wait is bounded; a wait that runs out latches
+// kDevTimeout in the device error word instead of spinning forever.
+//
+// The same overlap-add + scan finishes the schoolboy and by-digit products
+// (src/mpz-ram.lisp:367-431), with V_i = sum_j x_(i-j) y_j.
+#include "hg_internal.h"
+
+namespace hg {
+namespace {
+
+constexpr int kCarryThreads = 256;
+constexpr int kCarryPer = 8;
+constexpr int kCarryTile = kCarryThreads * kCarryPer;
+constexpr int kSpinLimit = 1 << 22;
+
+struct V3 {
+  uint64_t w0, w1, w2;
+};
+
+__device__ __forceinline__ void add128_to(V3 &acc, uint64_t lo, uint64_t hi) {
+  const uint64_t s0 = acc.w0 + lo;
+  const uint64_t c0 = s0 < lo;
+  const uint64_t t1 = acc.w1 + hi;
+  const uint64_t c1 = t1 < hi;
+  const uint64_t s1 = t1 + c0;
+  const uint64_t c2 = s1 < c0;
+  acc.w0 = s0;
+  acc.w1 = s1;
+  acc.w2 += c1 + c2;
+}
+
+struct CrtProducer {
+  const uint64_t *res;  // [3][N] natural-order residues from the unscaled inverse
+  uint64_t n;           // N
+  CrtConst k;
+
+  __device__ __forceinline__ V3 operator()(uint64_t i) const {
+    const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
+    const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
+    const uint64_t r0 = res[i], r1 = res[n + i], r2 = res[2 * n + i];
+    const uint64_t y0 = mont_mul(r0, k.k0, p0, c0);
+    const uint64_t t1 = sub_mod(mont_mul(r1, k.k1a, p1, c1), mont_mul(y0, k.k1b, p1, c1), p1);
+    uint64_t t2 = sub_mod(mont_mul(r2, k.k2a, p2, c2), mont_mul(y0, k.k2b, p2, c2), p2);
+    t2 = sub_mod(t2, mont_mul(t1, k.k2c, p2, c2), p2);
+    // V = y0 + p0 t1 + (p0 p1) t2 < p0 p1 p2 < 2^188
+    V3 v{y0, 0, 0};
+    add128_to(v, p0 * t1, __umul64hi(p0, t1));
+    const uint64_t a0 = k.p01_lo * t2, a1 = __umul64hi(k.p01_lo, t2);
+    const uint64_t b0 = k.p01_hi * t2, b1 = __umul64hi(k.p01_hi, t2);
+    // (p0p1) t2 = a0 + (a1 + b0) 2^64 + b1 2^128
+    const uint64_t m1 = a1 + b0;
+    const uint64_t mc = m1 < a1;
+    add128_to(v, a0, m1);
+    v.w2 += b1 + mc;
+    return v;
+  }
+};
+
+struct ConvProducer {
+  const uint64_t *x;
+  uint64_t nx;
+  const uint64_t *y;  // null: multiply by dval
+  uint64_t ny;
+  uint64_t dval;
+
+  __device__ __forceinline__ V3 operator()(uint64_t i) const {
+    V3 v{0, 0, 0};
+    if (!y) {
+      if (i < nx) {
+        const uint64_t a = x[i];
+        v.w0 = a * dval;
+        v.w1 = __umul64hi(a, dval);
+      }
+      return v;
+    }
+    const uint64_t jlo = i >= nx ? i - nx + 1 : 0;
+    const uint64_t jhi = i < ny - 1 ? i : ny - 1;
+    for (uint64_t j = jlo; j <= jhi; ++j) {
+      const uint64_t a = x[i - j], b = y[j];
+      add128_to(v, a * b, __umul64hi(a, b));
+    }
+    return v;
+  }
+};
+
+__device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t state, uint32_t g, uint32_t p) {
+  return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | state;
+}
+
+// Carry into the tile from all earlier tiles.  Publishes this tile's
+// aggregate first so that later tiles can proceed.
+__device__ uint32_t look_back(const ScanState &ss, uint64_t tile, GP agg) {
+  volatile unsigned long long *flags = ss.flags;
+  if (tile == 0) return 0;
+  __threadfence();
+  flags[tile] = flag_word(ss.epoch, 1, agg.g, agg.p);
+  GP acc{0, 1};  // identity: carry passes through
+  int64_t j = static_cast<int64_t>(tile) - 1;
+  while (j >= 0) {
+    unsigned long long w;
+    int spins = 0;
+    for (;;) {
+      w = flags[j];
+      if ((w >> 32) == ss.epoch && (w & 3u)) break;
+      if (++spins >= kSpinLimit) {
+        atomicCAS(ss.err, kDevOk, kDevTimeout);
+        return 0;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    const uint32_t g = static_cast<uint32_t>((w >> 2) & 1u), p = static_cast<uint32_t>((w >> 3) & 1u);
+    if ((w & 3u) == 2u) return acc.g | (acc.p & g);  // inclusive carry of tile j
+    acc = gp_compose(GP{g, p}, acc);                  // prepend tile j's run
+    --j;
+  }
+  return acc.g;
+}
+
+template <class Producer>
+__global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer prod, uint64_t *__restrict__ out,
+                                                              uint64_t nproc, ScanState ss) {
+  __shared__ uint64_t s_prev[kCarryThreads][9];
+  __shared__ GP s_warp[kCarryThreads / 32];
+  __shared__ unsigned long long s_tile;
+  __shared__ uint32_t s_cin;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  if (tid == 0) s_tile = atomicAdd(ss.ticket, 1ull) - ss.ticket_base;
+  __syncthreads();
+  const uint64_t tile = s_tile;
+  if (tile >= gridDim.x) {  // ticket out of step with this launch: touch nothing
+    if (tid == 0) atomicCAS(ss.err, kDevOk, kDevTicket);
+    return;
+  }
+  const uint64_t i0 = tile * kCarryTile + static_cast<uint64_t>(tid) * kCarryPer;
+
+  V3 v[kCarryPer];
+#pragma unroll
+  for (int k = 0; k < kCarryPer; ++k) v[k] = (i0 + k < nproc) ? prod(i0 + k) : V3{0, 0, 0};
+  s_prev[tid][0] = v[5].w0; s_prev[tid][1] = v[5].w1; s_prev[tid][2] = v[5].w2;
+  s_prev[tid][3] = v[6].w0; s_prev[tid][4] = v[6].w1; s_prev[tid][5] = v[6].w2;
+  s_prev[tid][6] = v[7].w0; s_prev[tid][7] = v[7].w1; s_prev[tid][8] = v[7].w2;
+  V3 pm3{0, 0, 0}, pm2{0, 0, 0}, pm1{0, 0, 0};
+  if (tid == 0 && i0 >= 3) {
+    pm3 = prod(i0 - 3);
+    pm2 = prod(i0 - 2);
+    pm1 = prod(i0 - 1);
+  }
+  __syncthreads();
+  if (tid > 0) {
+    pm3 = V3{s_prev[tid - 1][0], s_prev[tid - 1][1], s_prev[tid - 1][2]};
+    pm2 = V3{s_prev[tid - 1][3], s_prev[tid - 1][4], s_prev[tid - 1][5]};
+    pm1 = V3{s_prev[tid - 1][6], s_prev[tid - 1][7], s_prev[tid - 1][8]};
+  }
+
+  // W_i = v0_i + v1_(i-1) + v2_(i-2) = wl + wh 2^64 (wh <= 2); then
+  // A_i = wl_i + wh_(i-1) = al + ah 2^64 (ah <= 1).
+  auto wsum = [](uint64_t a, uint64_t b, uint64_t c, uint64_t &hi) {
+    const uint64_t s = a + b;
+    uint64_t h = s < a;
+    const uint64_t t = s + c;
+    h += t < s;
+    hi = h;
+    return t;
+  };
+  uint64_t whp;
+  (void)wsum(pm1.w0, pm2.w1, pm3.w2, whp);  // W_(i0-1)
+  uint64_t al[kCarryPer];
+  uint32_t gbits = 0, pbits = 0;
+#pragma unroll
+  for (int k = 0; k < kCarryPer; ++k) {
+    const V3 &c1 = (k >= 1) ? v[k - 1] : pm1;
+    const V3 &c2 = (k >= 2) ? v[k - 2] : (k == 1 ? pm1 : pm2);
+    uint64_t wh;
+    const uint64_t wl = wsum(v[k].w0, c1.w1, c2.w2, wh);
+    const uint64_t a = wl + whp;
+    const uint32_t ah = a < wl;
+    al[k] = a;
+    gbits |= ah << k;
+    pbits |= ((a == ~0ull) && !ah ? 1u : 0u) << k;
+    whp = wh;
+  }
+  // Thread aggregate over its 8 positions (position 0 least significant).
+  GP t{0, 1};
+#pragma unroll
+  for (int k = 0; k < kCarryPer; ++k) t = gp_compose(t, GP{(gbits >> k) & 1u, (pbits >> k) & 1u});
+
+  // Inclusive warp scan, then across warps.
+  GP inc = t;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t og = __shfl_up_sync(0xffffffffu, inc.g, d);
+    const uint32_t op = __shfl_up_sync(0xffffffffu, inc.p, d);
+    if (lane >= d) inc = gp_compose(GP{og, op}, inc);
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  GP wpre{0, 1};
+  for (int w = 0; w < wid; ++w) wpre = gp_compose(wpre, s_warp[w]);
+  GP excl;
+  {
+    const uint32_t og = __shfl_up_sync(0xffffffffu, inc.g, 1);
+    const uint32_t op = __shfl_up_sync(0xffffffffu, inc.p, 1);
+    excl = lane == 0 ? GP{0, 1} : GP{og, op};
+  }
+  excl = gp_compose(wpre, excl);  // runs over positions before this thread, within the tile
+  if (tid == 0) {
+    GP agg{0, 1};
+    for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
+    const uint32_t cin = look_back(ss, tile, agg);
+    const uint32_t cout = agg.g | (agg.p & cin);
+    __threadfence();
+    reinterpret_cast<volatile unsigned long long *>(ss.flags)[tile] = flag_word(ss.epoch, 2, cout, 0);
+    s_cin = cin;
+    const uint64_t last = tile * kCarryTile + kCarryTile;
+    if (last >= nproc && tile * kCarryTile < nproc && cout) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
+  }
+  __syncthreads();
+  uint32_t cin = excl.g | (excl.p & s_cin);
+#pragma unroll
+  for (int k = 0; k < kCarryPer; ++k) {
+    const uint64_t i = i0 + k;
+    const uint64_t z = al[k] + cin;
+    cin = ((gbits >> k) & 1u) | (((pbits >> k) & 1u) & cin);
+    if (i < nproc) out[i] = z;
+  }
+}
+
+}  // namespace
+
+uint64_t carry_tiles(uint64_t n) { return (n + kCarryTile - 1) / kCarryTile; }
+
+cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, uint64_t *out, uint64_t nout,
+                             const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
+  const uint64_t n = 1ull << logN;
+  const uint64_t nproc = nout < n ? nout : n;
+  const uint64_t tiles = carry_tiles(nproc);
+  *tiles_used = tiles;
+  if (tiles == 0) return cudaSuccess;
+  CrtProducer prod{res, n, cc};
+  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,
+                                   uint64_t nout, const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
+  const uint64_t nproc = nout < nx + ny ? nout : nx + ny;
+  const uint64_t tiles = carry_tiles(nproc);
+  *tiles_used = tiles;
+  if (tiles == 0) return cudaSuccess;
+  ConvProducer prod{x, nx, y, ny, 0};
+  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,
+                               const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
+  const uint64_t nproc = nout < nx + 1 ? nout : nx + 1;
+  const uint64_t tiles = carry_tiles(nproc);
+  *tiles_used = tiles;
+  if (tiles == 0) return cudaSuccess;
+  ConvProducer prod{x, nx, nullptr, 1, d};
+  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

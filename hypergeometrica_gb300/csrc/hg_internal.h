@@ -1,0 +1,76 @@
+// hg_internal.h -- structures shared by the kernels and the host driver.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hg_common.cuh"
+
+namespace hg {
+
+// Device twiddle tables of one prime, all in Montgomery form.
+struct NttTables {
+  const uint64_t *sub_fwd;  // w_4096^e, e < 2048     (sub-transform twiddles, any R <= 4096)
+  const uint64_t *sub_inv;  // w_4096^-e
+  const uint64_t *hi_fwd;   // w_{2^30}^(e * 2^15), e < 2^15
+  const uint64_t *lo_fwd;   // w_{2^30}^e,          e < 2^15
+  const uint64_t *hi_inv;
+  const uint64_t *lo_inv;
+};
+
+// One NTT pass over a batch of (operand, prime) arrays.  The N residues of
+// an array form blocks of M = R*S; the pass performs the reference's
+// radix-2 stages subn = M .. 2S, i.e. an R-point transform down each of the
+// S columns of every block, followed (forward) or preceded (inverse) by the
+// twiddle w_M^(s * bitrev(r)).
+struct PassArgs {
+  uint64_t *data[2];         // residues per operand, [kPrimes][N]
+  const uint64_t *limbs[2];  // first forward pass: read limbs and reduce
+  uint64_t nlimbs[2];
+  int nops;                  // operands handled by this launch
+  int logN;
+  int logR;                  // log2 rows (transform points) of this pass
+  int logS;                  // log2 stride; 0 = contiguous pass
+  int logT;                  // log2 residues per tile
+  int prime_lo, nprimes;
+  uint64_t prime_stride;     // words between the arrays of consecutive primes
+  uint64_t tiles;            // tiles per (operand, prime)
+  PrimeConst pc[kPrimes];
+  NttTables tb[kPrimes];
+};
+
+// Constants of the Garner reconstruction for one transform length.
+struct CrtConst {
+  PrimeConst pc[kPrimes];
+  uint64_t k0;             // Mont(N^-1 * 2^64)                    mod p0
+  uint64_t k1a, k1b;       // Mont(N^-1 2^64 p0^-1), Mont(p0^-1)    mod p1
+  uint64_t k2a, k2b, k2c;  // Mont(N^-1 2^64 (p0p1)^-1), Mont((p0p1)^-1), Mont(p1^-1) mod p2
+  uint64_t p01_lo, p01_hi; // p0 * p1
+};
+
+// Carry-scan launch state (decoupled look-back across tiles).
+struct ScanState {
+  unsigned long long *ticket;  // monotonically increasing tile ticket
+  unsigned long long ticket_base;
+  unsigned long long *flags;   // one word per tile
+  uint32_t epoch;              // distinguishes launches sharing `flags`
+  int *err;                    // device error word
+};
+
+// Kernel launchers (hg_ntt.cu, hg_crt.cu).
+cudaError_t launch_ntt_pass(const PassArgs &a, bool inverse, cudaStream_t st);
+cudaError_t launch_pointwise(uint64_t *a, const uint64_t *b, int logN, const PrimeConst *pc, bool square,
+                             cudaStream_t st);
+cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, uint64_t *out, uint64_t nout,
+                             const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
+cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,
+                                   uint64_t nout, const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
+cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,
+                               const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
+cudaError_t launch_scale(uint64_t *a, uint64_t n, uint64_t mont_factor, PrimeConst pc, cudaStream_t st);
+
+// Tiles a carry-scan launch over n positions uses.
+uint64_t carry_tiles(uint64_t n);
+
+}  // namespace hg

@@ -1,0 +1,55 @@
+"""Device-memory entry points on torch tensors (uint64 stored as int64).
+
+torch provides the device allocations and the stream; the arithmetic runs in
+libhg_gb300.so.  Tensors must be contiguous int64 CUDA tensors holding the
+64-bit limbs bit for bit.
+"""
+
+from __future__ import annotations
+
+from ._lib import check, load
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _p(t):
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def mul(x, y, out, nx=None, ny=None, stream=None) -> None:
+    """|x| * |y| into out (hg_mul_device); sizes default to the tensor lengths."""
+    nx = x.numel() if nx is None else nx
+    ny = y.numel() if ny is None else ny
+    check(load().hg_mul_device(_p(x), nx, _p(y), ny, _p(out), out.numel(), _stream(stream)))
+
+
+def sqr(x, out, nx=None, stream=None) -> None:
+    nx = x.numel() if nx is None else nx
+    check(load().hg_sqr_device(_p(x), nx, _p(out), out.numel(), _stream(stream)))
+
+
+def mul_schoolboy(x, y, out, stream=None) -> None:
+    check(load().hg_mul_schoolboy_device(_p(x), x.numel(), _p(y), y.numel(), _p(out), out.numel(), _stream(stream)))
+
+
+def ntt_forward(a, mod_num: int, stream=None) -> None:
+    """ntt-forward in place (bit-reversed output)."""
+    check(load().hg_ntt_forward_device(_p(a), a.numel(), mod_num, _stream(stream)))
+
+
+def ntt_reverse(a, mod_num: int, stream=None) -> None:
+    """ntt-reverse in place (bit-reversed input, natural output, 1/N)."""
+    check(load().hg_ntt_reverse_device(_p(a), a.numel(), mod_num, _stream(stream)))
+
+
+def sync(stream=None) -> None:
+    """Wait and surface device-side errors (hg_sync)."""
+    check(load().hg_sync(None if stream is None else _stream(stream)))

@@ -1,0 +1,150 @@
+/*
+ * hypergeometrica_gb300.h -- C ABI of the GB300 exact multiplication library.
+ *
+ * This is the drop-in boundary for hypergeometrica's in-core multiplication
+ * path.  In the Common Lisp reference, MPZ multiplication goes through the
+ * generic mpz-* (src/mpz-protocol.lisp:74), whose method on two mpz/ram
+ * (src/multiply.lisp:12-49) picks by-digit, schoolboy, squaring
+ * (mpz-square, src/ntt-multiply.lisp:101-172) or the three-prime NTT product
+ * (src/ntt-multiply.lisp:174-254).  A CFFI binding replaces those functions
+ * with the entry points below; operands arrive as the raw uint64_t digit
+ * pointers that vec-digit-pointer hands out (src/vec.lisp:17-19), little-
+ * endian 64-bit limbs, magnitude only (the sign stays on the Lisp side).
+ *
+ * Conventions
+ *  - Every entry point returns HG_OK (0) or a negative HG_ERR_* code; the
+ *    message of the last failure on the calling thread is available from
+ *    hg_last_error().  There is no CPU fallback: a failure is an error.
+ *  - Sizes are limb counts.  High zero limbs of an operand are ignored
+ *    (mpz-size, src/vec.lisp:218-229).
+ *  - Products are exact.  out receives the magnitude in its low limbs and
+ *    zeros up to nout; nout must hold the product (at least nx + ny limbs).
+ *  - Host entry points take host pointers (pinned memory is fastest) and
+ *    return when out is written.  *_device entry points take device
+ *    pointers and a cudaStream_t (NULL = the legacy default stream), enqueue
+ *    work and return; errors detected on the device surface at the next
+ *    hg_sync().
+ *  - The library is thread-safe: host entry points serialise on an internal
+ *    lock; device entry points must not be called concurrently on the same
+ *    stream from two threads.
+ */
+#ifndef HYPERGEOMETRICA_GB300_H
+#define HYPERGEOMETRICA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_OK 0
+#define HG_ERR_ARG (-1)          /* bad argument (null pointer, nout too small, ...)        */
+#define HG_ERR_MODULI (-2)       /* the scheme cannot hold the convolution                  */
+                                 /* (num-moduli-needed-for-bits, src/moduli.lisp:362-364)   */
+#define HG_ERR_OOM (-3)          /* device or pinned memory exhausted                        */
+#define HG_ERR_CUDA (-4)         /* a CUDA runtime call failed                               */
+#define HG_ERR_INCONSISTENT (-5) /* a carry ran past the result storage                      */
+                                 /* (add-big-digit, src/ntt-multiply.lisp:19-22)            */
+#define HG_ERR_TIMEOUT (-6)      /* a bounded device wait gave up; results are invalid       */
+#define HG_ERR_NOT_INIT (-7)     /* hg_init failed or was given foreign moduli               */
+
+/* Library initialisation.  Replaces the load-time construction of the
+ * global **scheme** (src/ntt-multiply.lisp:8, make-modular-scheme of
+ * default-moduli, src/moduli.lisp:257-353).  moduli/k may be NULL/0 to
+ * accept the built-in scheme; otherwise they must be the reference's scheme
+ * moduli (any order), which the library checks against its own tables.
+ * device selects the CUDA device (-1 = current).  Called implicitly by the
+ * first entry point when not called explicitly. */
+int hg_init(const uint64_t *moduli, int k, int device);
+
+/* Release every device buffer, stream and table held by the library. */
+int hg_shutdown(void);
+
+/* Copy the message of the last error on this thread into buf. */
+int hg_last_error(char *buf, size_t len);
+
+/* Number of moduli and their values, largest first (scheme-moduli). */
+int hg_scheme_moduli(uint64_t *out, int cap);
+
+// Transform length mpz-*/ntt uses for trimmed sizes nx, ny: the least power
+// of two >= nx + ny (src/ntt-multiply.lisp:175-176).  mpz-square uses
+// hg_ntt_length(nx, nx) (:103).
+size_t hg_ntt_length(size_t nx, size_t ny);
+
+/* ---- products on host memory ------------------------------------------ */
+
+// mpz-*/ntt (src/ntt-multiply.lisp:174-254): |x| * |y| through the three-prime
+// NTT.  Replaces the Lisp function of that name.
+int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout);
+
+/* mpz-square (src/ntt-multiply.lisp:101-172): |x|^2. */
+int hg_sqr(const uint64_t *x, size_t nx, uint64_t *out, size_t nout);
+
+/* %multiply-storage/schoolboy (src/mpz-ram.lisp:404-431): |x| * |y| by the
+ * quadratic method, used by mpz-* when the smaller operand has at most
+ * *ntt-multiply-threshold* limbs (src/multiply.lisp:37-42). */
+int hg_mul_schoolboy(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout);
+
+/* mpz-multiply-by-digit! (src/mpz-ram.lisp:367-395) as mpz-* uses it for a
+ * one-limb operand (src/multiply.lisp:23-36): |x| * d. */
+int hg_mul_digit(const uint64_t *x, size_t nx, uint64_t d, uint64_t *out, size_t nout);
+
+/* The whole mpz-* method on two mpz/ram (src/multiply.lisp:12-49), signs
+ * included: zero, by-digit, schoolboy (smaller operand <= threshold limbs),
+ * squaring when same_object (the (eq x y) test), else the NTT product.
+ * Writes the trimmed magnitude to out, its length to *nres and the sign
+ * (+1/-1; +1 for zero) to *sres.  sx, sy are +1 or -1. */
+int hg_mpz_mul(const uint64_t *x, size_t nx, int sx, const uint64_t *y, size_t ny, int sy, int same_object,
+               size_t threshold, uint64_t *out, size_t nout, size_t *nres, int *sres);
+
+/* ---- products on device memory ---------------------------------------- */
+
+/* hg_mul / hg_sqr / hg_mul_schoolboy on device pointers, enqueued on stream. */
+int hg_mul_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
+                  void *stream);
+int hg_sqr_device(const uint64_t *x, size_t nx, uint64_t *out, size_t nout, void *stream);
+int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out,
+                            size_t nout, void *stream);
+
+/* Wait for the library's work on stream (NULL = all of it) and report any
+ * error latched on the device since the last hg_sync. */
+int hg_sync(void *stream);
+
+/* ---- spectra (parity hooks) -------------------------------------------- */
+
+/* ntt-forward (src/number-theoretic-transform.lisp:40-90) in place on n
+ * device residues (each < the modulus) for scheme modulus mod_num: natural
+ * order in, bit-reversed order out, the same values the reference computes. */
+int hg_ntt_forward_device(uint64_t *a, size_t n, int mod_num, void *stream);
+
+/* ntt-reverse (src/number-theoretic-transform.lisp:93-143) in place:
+ * bit-reversed in, natural out, scaled by 1/n like the reference. */
+int hg_ntt_reverse_device(uint64_t *a, size_t n, int mod_num, void *stream);
+
+/* ---- instrumentation ---------------------------------------------------
+ * No counterpart in the reference (its *verbose* stage timers,
+ * src/ntt-multiply.lisp:109-114, print wall-clock milliseconds).  Kernel
+ * classes index the arrays below. */
+#define HG_KC_NTT_FORWARD 0 /* forward NTT passes (the first also reduces limbs) */
+#define HG_KC_NTT_INVERSE 1 /* inverse NTT passes                               */
+#define HG_KC_POINTWISE 2   /* pointwise product / square                       */
+#define HG_KC_CARRY 3       /* reconstruction + carry scan                      */
+#define HG_KC_SMALL 4       /* schoolboy / by-digit products                    */
+#define HG_KC_OTHER 5       /* scaling and other helpers                        */
+#define HG_KC_COUNT 6
+
+/* Record a CUDA event pair around every kernel launch from now on (on != 0)
+ * or stop recording (on == 0). */
+int hg_profile_enable(int on);
+
+/* Totals per kernel class since the last read, then reset: launches, device
+ * milliseconds (only while recording) and the algorithmic bytes those
+ * launches move (each input read once, each output written once).
+ * Synchronises on the recorded events. */
+int hg_profile_read(uint64_t *launches, double *ms, double *bytes, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
