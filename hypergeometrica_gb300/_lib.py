@@ -72,7 +72,7 @@ SIGNATURES = {
                                        ctypes.c_int]),
 }
 
-KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "pointwise", "carry", "small", "other"]
+KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "middle", "carry", "small", "other"]
 
 
 def profile_enable(on: bool) -> None:

@@ -291,24 +291,29 @@ struct PassPlan {
   int logR, logS, logT;
 };
 
-// Passes for N = 2^L: strided passes of at most 8 rows-bits (tiles of 4096
-// residues with >= 16 columns, i.e. >= 128-byte row segments), then one
-// contiguous pass over 4096-residue blocks.
+// Passes for N = 2^L: strided passes of 4..8 row bits over 4096-residue tiles
+// (>= 16 columns, i.e. >= 128-byte row segments), then one contiguous pass
+// over blocks of 2^T <= 4096 residues.  The last entry is the contiguous one.
 std::vector<PassPlan> plan_passes(int L) {
   std::vector<PassPlan> v;
   if (L <= kTileBits) {
     v.push_back({L, 0, L});
     return v;
   }
-  const int rem = L - kTileBits;
-  const int k = (rem + 7) / 8;
+  std::vector<int> parts;
+  if (L < kTileBits + 4) {
+    parts.push_back(4);  // 13..15: one 4-bit strided pass, a 9..11-bit block
+  } else {
+    const int rem = L - kTileBits;
+    const int k = (rem + 7) / 8;
+    for (int i = 0; i < k; ++i) parts.push_back(rem / k + (i < rem % k ? 1 : 0));
+  }
   int logS = L;
-  for (int i = 0; i < k; ++i) {
-    const int part = rem / k + (i < rem % k ? 1 : 0);
+  for (int part : parts) {
     logS -= part;
     v.push_back({part, logS, kTileBits});
   }
-  v.push_back({kTileBits, 0, kTileBits});
+  v.push_back({logS, 0, logS});
   return v;
 }
 
@@ -326,29 +331,47 @@ PassArgs base_args(int L, int nops) {
   return a;
 }
 
-cudaError_t run_passes(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
-  const int np = static_cast<int>(plan.size());
+// Algorithmic bytes of a launch over nops operands: every residue written
+// once, every input read once (limbs when a pass reduces them itself).
+double pass_bytes(const PassArgs &a, int readers, int writers) {
+  const double words = static_cast<double>(a.nprimes) * static_cast<double>(uint64_t(1) << a.logN);
+  double bytes = 8.0 * words * writers;
+  for (int op = 0; op < readers; ++op)
+    bytes += a.limbs[op] ? 8.0 * static_cast<double>(a.nlimbs[op]) : 8.0 * words;
+  return bytes;
+}
+
+// The strided passes of `plan` (all but its last entry), forward in order or
+// inverse in reverse order.
+cudaError_t run_strided(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
+  const int np = static_cast<int>(plan.size()) - 1;
   for (int s = 0; s < np; ++s) {
     const PassPlan &pp = plan[inverse ? np - 1 - s : s];
     a.logR = pp.logR;
     a.logS = pp.logS;
     a.logT = pp.logT;
     a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
-    // Algorithmic bytes: each residue read and written once; the first
-    // forward pass reads limbs instead of residues.
-    const double words = static_cast<double>(a.nprimes) * static_cast<double>(uint64_t(1) << a.logN);
-    double bytes = 0;
-    for (int op = 0; op < a.nops; ++op)
-      bytes += 8.0 * words + (a.limbs[op] ? 8.0 * static_cast<double>(a.nlimbs[op]) : 8.0 * words);
     cudaError_t e;
     {
-      ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, bytes);
-      e = launch_ntt_pass(a, inverse, st);
+      ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, pass_bytes(a, a.nops, a.nops));
+      e = launch_ntt_strided(a, inverse, st);
     }
     if (e != cudaSuccess) return e;
     a.limbs[0] = a.limbs[1] = nullptr;  // only the first forward pass reads limbs
   }
   return cudaSuccess;
+}
+
+// The contiguous pass (the plan's last entry) in the given mode.
+cudaError_t run_contig(PassArgs a, const PassPlan &pp, int mode, cudaStream_t st) {
+  a.logR = pp.logR;
+  a.logS = 0;
+  a.logT = pp.logT;
+  a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
+  const int readers = mode == kContigMul ? 2 : 1;
+  const int cls = mode == kContigFwd ? HG_KC_NTT_FORWARD : (mode == kContigInv ? HG_KC_NTT_INVERSE : HG_KC_MIDDLE);
+  ProfScope ps(cls, st, pass_bytes(a, readers, 1));
+  return launch_ntt_contig(a, mode, st);
 }
 
 CrtConst crt_const(int L) {
@@ -430,22 +453,25 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     HG_CUDA(c.A.ensure(words * 8), "workspace allocation");
     if (!square) HG_CUDA(c.B.ensure(words * 8), "workspace allocation");
   }
+  // Strided forward passes, the fused middle (last forward pass of both
+  // operands + pointwise product + first inverse pass), strided inverse passes.
   const std::vector<PassPlan> plan = plan_passes(L);
   PassArgs a = base_args(L, square ? 1 : 2);
   a.data[0] = c.A.u64();
   a.data[1] = c.B.u64();
   a.limbs[0] = x;
-  a.limbs[1] = y;
+  a.limbs[1] = square ? nullptr : y;
   a.nlimbs[0] = nx;
-  a.nlimbs[1] = ny;
-  HG_CUDA(run_passes(a, plan, false, st), "forward transform");
+  a.nlimbs[1] = square ? 0 : ny;
+  HG_CUDA(run_strided(a, plan, false, st), "forward transform");
   {
-    ProfScope ps(HG_KC_POINTWISE, st, 8.0 * static_cast<double>(words) * (square ? 2 : 3));
-    HG_CUDA(launch_pointwise(c.A.u64(), square ? nullptr : c.B.u64(), L, c.pc, square, st), "pointwise product");
+    PassArgs m = a;
+    if (plan.size() > 1) m.limbs[0] = m.limbs[1] = nullptr;
+    HG_CUDA(run_contig(m, plan.back(), square ? kContigSqr : kContigMul, st), "middle pass");
   }
   PassArgs inv = base_args(L, 1);
   inv.data[0] = c.A.u64();
-  HG_CUDA(run_passes(inv, plan, true, st), "inverse transform");
+  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
   if (nout > N) HG_CUDA(cudaMemsetAsync(out + N, 0, (nout - N) * sizeof(uint64_t), st), "zero tail");
   ScanState ss;
   const uint64_t nproc = nout < N ? nout : N;
@@ -566,7 +592,14 @@ int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) 
   pa.prime_lo = mod_num;
   pa.nprimes = 1;
   pa.prime_stride = 0;
-  HG_CUDA(run_passes(pa, plan_passes(L), inverse, st), "transform");
+  const std::vector<PassPlan> plan = plan_passes(L);
+  if (!inverse) {
+    HG_CUDA(run_strided(pa, plan, false, st), "forward transform");
+    HG_CUDA(run_contig(pa, plan.back(), kContigFwd, st), "forward transform");
+  } else {
+    HG_CUDA(run_contig(pa, plan.back(), kContigInv, st), "inverse transform");
+    HG_CUDA(run_strided(pa, plan, true, st), "inverse transform");
+  }
   if (inverse) {
     const uint64_t p = g_ctx.moduli[mod_num];
     ProfScope ps(HG_KC_OTHER, st, 16.0 * static_cast<double>(n));

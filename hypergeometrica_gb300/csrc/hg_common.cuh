@@ -39,14 +39,18 @@ enum DevErr : int {
   kDevTicket = 3,         // a carry-scan tile ticket fell outside its launch
 };
 
+// All residues are < p < 2^63, so a difference of two of them, or a sum
+// minus p, lies in (-2^63, 2^63): its sign bit says whether to add p back.
+__host__ __device__ __forceinline__ uint64_t fix_neg(uint64_t t, uint64_t p) {
+  return t + (p & static_cast<uint64_t>(static_cast<int64_t>(t) >> 63));
+}
+
 __host__ __device__ __forceinline__ uint64_t add_mod(uint64_t a, uint64_t b, uint64_t p) {
-  uint64_t s = a + b;  // a, b < p < 2^63
-  return s >= p ? s - p : s;
+  return fix_neg(a + b - p, p);
 }
 
 __host__ __device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uint64_t p) {
-  uint64_t d = a - b;
-  return a < b ? d + p : d;
+  return fix_neg(a - b, p);
 }
 
 __device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __umul64hi(a, b); }
@@ -63,8 +67,7 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
   const uint64_t t = static_cast<uint64_t>(static_cast<uint32_t>(m)) * c + (m >> kShift);
   const uint64_t u = (m >> 32) * c + (t >> 32);
   const uint64_t mph = (u << 23) | (static_cast<uint32_t>(t) >> 9);
-  const uint64_t r = hi - mph;  // low halves cancel exactly
-  return hi < mph ? r + p : r;
+  return fix_neg(hi - mph, p);  // low halves cancel exactly; hi, mph < p
 }
 
 // x mod p for any 64-bit x (x < 4p because p > 2^62).

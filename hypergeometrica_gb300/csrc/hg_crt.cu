@@ -45,10 +45,33 @@ struct CrtProducer {
   uint64_t n;           // N
   CrtConst k;
 
-  __device__ __forceinline__ V3 operator()(uint64_t i) const {
+  __device__ __forceinline__ V3 operator()(uint64_t i) const { return garner(res[i], res[n + i], res[2 * n + i]); }
+
+  // Eight consecutive positions from i0 (a multiple of 8): 16-byte loads.
+  __device__ __forceinline__ void eight(uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+    if (i0 + 8 <= nproc) {
+      uint64_t r[3][8];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(res + j * n + i0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const ulonglong2 w = __ldg(src + q);
+          r[j][2 * q] = w.x;
+          r[j][2 * q + 1] = w.y;
+        }
+      }
+#pragma unroll
+      for (int k8 = 0; k8 < 8; ++k8) v[k8] = garner(r[0][k8], r[1][k8], r[2][k8]);
+    } else {
+#pragma unroll
+      for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? (*this)(i0 + k8) : V3{0, 0, 0};
+    }
+  }
+
+  __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
-    const uint64_t r0 = res[i], r1 = res[n + i], r2 = res[2 * n + i];
     const uint64_t y0 = mont_mul(r0, k.k0, p0, c0);
     const uint64_t t1 = sub_mod(mont_mul(r1, k.k1a, p1, c1), mont_mul(y0, k.k1b, p1, c1), p1);
     uint64_t t2 = sub_mod(mont_mul(r2, k.k2a, p2, c2), mont_mul(y0, k.k2b, p2, c2), p2);
@@ -73,6 +96,11 @@ struct ConvProducer {
   const uint64_t *y;  // null: multiply by dval
   uint64_t ny;
   uint64_t dval;
+
+  __device__ __forceinline__ void eight(uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+#pragma unroll
+    for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? (*this)(i0 + k8) : V3{0, 0, 0};
+  }
 
   __device__ __forceinline__ V3 operator()(uint64_t i) const {
     V3 v{0, 0, 0};
@@ -147,8 +175,7 @@ __global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer pro
   const uint64_t i0 = tile * kCarryTile + static_cast<uint64_t>(tid) * kCarryPer;
 
   V3 v[kCarryPer];
-#pragma unroll
-  for (int k = 0; k < kCarryPer; ++k) v[k] = (i0 + k < nproc) ? prod(i0 + k) : V3{0, 0, 0};
+  prod.eight(i0, nproc, v);
   s_prev[tid][0] = v[5].w0; s_prev[tid][1] = v[5].w1; s_prev[tid][2] = v[5].w2;
   s_prev[tid][3] = v[6].w0; s_prev[tid][4] = v[6].w1; s_prev[tid][5] = v[6].w2;
   s_prev[tid][6] = v[7].w0; s_prev[tid][7] = v[7].w1; s_prev[tid][8] = v[7].w2;

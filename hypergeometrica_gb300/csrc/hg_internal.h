@@ -59,9 +59,12 @@ struct ScanState {
 };
 
 // Kernel launchers (hg_ntt.cu, hg_crt.cu).
-cudaError_t launch_ntt_pass(const PassArgs &a, bool inverse, cudaStream_t st);
-cudaError_t launch_pointwise(uint64_t *a, const uint64_t *b, int logN, const PrimeConst *pc, bool square,
-                             cudaStream_t st);
+// Strided pass (hg_ntt_strided.cu): 4 <= logR <= 8, logT = 12.
+cudaError_t launch_ntt_strided(const PassArgs &a, bool inverse, cudaStream_t st);
+// Contiguous pass (hg_ntt_contig.cu), mode: 0 forward, 1 inverse, 2 product
+// of operands 0 and 1, 3 square of operand 0; logR == logT <= 12.
+constexpr int kContigFwd = 0, kContigInv = 1, kContigMul = 2, kContigSqr = 3;
+cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st);
 cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, uint64_t *out, uint64_t nout,
                              const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
 cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,

@@ -1,0 +1,303 @@
+// hg_ntt_contig.cu -- the contiguous NTT pass and the middle of a product.
+//
+// The last T <= 12 forward stages of the reference's transform (ntt-forward,
+// src/number-theoretic-transform.lisp:40-90) and the first T inverse stages
+// (ntt-reverse, :93-143) act on contiguous blocks of 2^T residues.  One CTA
+// owns one block.  Modes:
+//   kFwd  the forward stages only (spectrum hook; bit-reversed output),
+//   kInv  the inverse stages only (spectrum hook),
+//   kMul  both operands' forward stages, the pointwise product
+//         (multiply-pointwise!, src/ntt-multiply.lisp:88-99) and the
+//         inverse stages: the block is read once per operand, written once,
+//   kSqr  the same for one operand squared (src/ntt-multiply.lisp:136-144).
+// For transforms of at most 2^12 points this is the whole product's NTT work,
+// and the kernel reads the limbs and reduces them itself.
+//
+// The block runs in rounds of up to four stages on 16 registers per thread,
+// with one trip through shared memory between rounds; the stages of the low
+// row group use compile-time twiddles, and multiplications by 1 are skipped.
+// Transforms below 16 points run in ntt_tiny_kernel, one thread per prime.
+#include "hg_ntt_rounds.cuh"
+
+namespace hg {
+namespace {
+
+using namespace rounds;
+
+constexpr int kFwd = 0, kInv = 1, kMul = 2, kSqr = 3;
+
+// Register block of row group g in a 2^T block: groups of four row bits from
+// the bottom; the top group may be partial and then shares its register
+// block with the bits below it.
+template <int T>
+struct Groups {
+  static constexpr int G = (T + 3) / 4;
+  static constexpr int NBTOP = T - 4 * (G - 1);
+  template <int g>
+  __host__ __device__ static constexpr int A() { return g == G - 1 ? T - 4 : 4 * g; }
+  template <int g>
+  __host__ __device__ static constexpr int NB() { return g == G - 1 ? NBTOP : 4; }
+  template <int g>
+  __host__ __device__ static constexpr int JG() { return 4 - NB<g>(); }
+};
+
+template <int T, int g, bool INV>
+__device__ __forceinline__ void round_g(uint64_t (&v)[16], const uint64_t *tw, uint32_t xt, uint64_t p, uint32_t c) {
+  using Gr = Groups<T>;
+  constexpr int A = Gr::template A<g>();
+  constexpr int NB = Gr::template NB<g>();
+  constexpr int JG = Gr::template JG<g>();
+  constexpr bool TZERO = (g == 0) && (A == 0) && (JG == 0);
+  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO>(v, tw, xt, p, c);
+}
+
+// Move the thread's registers from the layout of group g to that of group h
+// through sm (two barriers: the buffer may still be read by the last round).
+template <int T, int g, int h>
+__device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_t &xt, uint32_t tid) {
+  using Gr = Groups<T>;
+  constexpr int Ag = Gr::template A<g>(), Ah = Gr::template A<h>();
+  if constexpr (Ag == Ah) return;
+  __syncthreads();
+  to_smem<Ag>(sm, v, xt);
+  __syncthreads();
+  xt = thread_base<Ah>(tid);
+  from_smem<Ah>(v, sm, xt);
+}
+
+// All forward rounds, from the top group down to group 0.
+template <int T>
+__device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, const uint64_t *tw, uint32_t &xt,
+                                               uint32_t tid, uint64_t p, uint32_t c) {
+  constexpr int G = Groups<T>::G;
+  if constexpr (G == 3) {
+    round_g<T, 2, false>(v, tw, xt, p, c);
+    regroup<T, 2, 1>(v, sm, xt, tid);
+    round_g<T, 1, false>(v, tw, xt, p, c);
+    regroup<T, 1, 0>(v, sm, xt, tid);
+    round_g<T, 0, false>(v, tw, xt, p, c);
+  } else if constexpr (G == 2) {
+    round_g<T, 1, false>(v, tw, xt, p, c);
+    regroup<T, 1, 0>(v, sm, xt, tid);
+    round_g<T, 0, false>(v, tw, xt, p, c);
+  } else {
+    round_g<T, 0, false>(v, tw, xt, p, c);
+  }
+}
+
+// All inverse rounds, from group 0 up to the top group.
+template <int T>
+__device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const uint64_t *tw, uint32_t &xt,
+                                               uint32_t tid, uint64_t p, uint32_t c) {
+  constexpr int G = Groups<T>::G;
+  round_g<T, 0, true>(v, tw, xt, p, c);
+  if constexpr (G >= 2) {
+    regroup<T, 0, 1>(v, sm, xt, tid);
+    round_g<T, 1, true>(v, tw, xt, p, c);
+  }
+  if constexpr (G == 3) {
+    regroup<T, 1, 2>(v, sm, xt, tid);
+    round_g<T, 2, true>(v, tw, xt, p, c);
+  }
+}
+
+template <int A>
+__device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *data, const uint64_t *limbs, uint64_t nl,
+                                           uint64_t base, uint32_t xt, uint64_t p) {
+  if (limbs) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const uint64_t o = base + (xt | (static_cast<uint32_t>(i) << A));
+      v[i] = o < nl ? reduce64(__ldg(limbs + o), p) : 0;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = data[base + (xt | (static_cast<uint32_t>(i) << A))];
+  }
+}
+
+template <int A>
+__device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *data, uint64_t base, uint32_t xt) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) data[base + (xt | (static_cast<uint32_t>(i) << A))] = v[i];
+}
+
+template <int T, int MODE>
+__global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassArgs P) {
+  using Gr = Groups<T>;
+  constexpr int ATOP = Gr::template A<Gr::G - 1>();
+  constexpr int A0 = Gr::template A<0>();
+  constexpr int NTHR = 1 << (T - 4);
+  constexpr uint32_t HALF = 1u << (T - 1);
+  extern __shared__ uint64_t smem[];
+  const uint32_t tid = threadIdx.x;
+  const int prime = P.prime_lo + static_cast<int>(blockIdx.x % P.nprimes);
+  const uint64_t tile = blockIdx.x / P.nprimes;
+  const uint64_t p = P.pc[prime].p;
+  const uint32_t c = P.pc[prime].c;
+  const NttTables tb = P.tb[prime];
+  const uint64_t poff = static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
+  const uint64_t base = tile << T;
+
+  constexpr bool TWO = (MODE == kMul);
+  constexpr bool NEED_F = (MODE != kInv), NEED_I = (MODE != kFwd);
+  uint64_t *smA = smem;
+  uint64_t *smB = smem + (TWO ? (1u << T) : 0u);
+  uint64_t *twf = smem + ((TWO ? 2u : 1u) << T);
+  uint64_t *twi = twf + (NEED_F ? HALF : 0u);
+  if (NEED_F) load_sub_twiddles(twf, tb.sub_fwd, T, tid, NTHR);
+  if (NEED_I) load_sub_twiddles(twi, tb.sub_inv, T, tid, NTHR);
+
+  uint64_t v[16];
+  uint32_t xt;
+  if constexpr (MODE == kInv) {
+    xt = thread_base<A0>(tid);
+    load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
+    __syncthreads();
+    inverse_rounds<T>(v, smA, twi, xt, tid, p, c);
+    store_block<ATOP>(v, P.data[0] + poff, base, xt);
+    return;
+  } else {
+    xt = thread_base<ATOP>(tid);
+    load_block<ATOP>(v, P.data[0] + poff, P.limbs[0], P.nlimbs[0], base, xt, p);
+    __syncthreads();
+    forward_rounds<T>(v, smA, twf, xt, tid, p, c);
+    if constexpr (MODE == kFwd) {
+      store_block<A0>(v, P.data[0] + poff, base, xt);
+      return;
+    } else {
+      if constexpr (MODE == kMul) {
+        // Park operand 0's spectrum in smA (each thread rereads only its own
+        // words), transform operand 1 through smB.
+        __syncthreads();
+        to_smem<A0>(smA, v, xt);
+        uint32_t xb = thread_base<ATOP>(tid);
+        load_block<ATOP>(v, P.data[1] + poff, P.limbs[1], P.nlimbs[1], base, xb, p);
+        forward_rounds<T>(v, smB, twf, xb, tid, p, c);
+        const uint32_t sx = swz(xb);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = mont_mul(smA[sx ^ swz(static_cast<uint32_t>(i) << A0)], v[i], p, c);
+        xt = xb;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
+      }
+      // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
+      inverse_rounds<T>(v, smA, twi, xt, tid, p, c);
+      store_block<ATOP>(v, P.data[0] + poff, base, xt);
+    }
+  }
+}
+
+// Transforms of 2, 4 or 8 points: the reference's loops, one thread per prime.
+__global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
+  const int prime = P.prime_lo + static_cast<int>(blockIdx.x % P.nprimes);
+  const uint64_t p = P.pc[prime].p;
+  const uint32_t c = P.pc[prime].c;
+  const NttTables tb = P.tb[prime];
+  const uint64_t poff = static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
+  const int L = P.logN;
+  const int n = 1 << L;
+  uint64_t a[2][8];
+  const int nops = mode == kMul ? 2 : 1;
+  for (int op = 0; op < nops; ++op)
+    for (int i = 0; i < n; ++i)
+      a[op][i] = P.limbs[op] ? (static_cast<uint64_t>(i) < P.nlimbs[op] ? reduce64(P.limbs[op][i], p) : 0)
+                             : P.data[op][poff + i];
+  if (mode != kInv) {
+    for (int op = 0; op < nops; ++op)
+      for (int ls = L; ls >= 1; --ls) {  // DIF, subn = 2^ls
+        const int half = 1 << (ls - 1);
+        for (int j = 0; j < half; ++j) {
+          const uint64_t w = tb.sub_fwd[static_cast<uint64_t>(j) << (kTileBits - ls)];
+          for (int r = 0; r < n; r += 2 * half) {
+            const uint64_t u = a[op][r + j], x = a[op][r + j + half];
+            a[op][r + j] = add_mod(u, x, p);
+            a[op][r + j + half] = mont_mul(u - x + p, w, p, c);
+          }
+        }
+      }
+  }
+  if (mode == kMul || mode == kSqr)
+    for (int i = 0; i < n; ++i) a[0][i] = mont_mul(a[0][i], a[mode == kMul ? 1 : 0][i], p, c);
+  if (mode != kFwd) {
+    for (int ls = 1; ls <= L; ++ls) {  // DIT, subn = 2^ls
+      const int half = 1 << (ls - 1);
+      for (int j = 0; j < half; ++j) {
+        const uint64_t w = tb.sub_inv[static_cast<uint64_t>(j) << (kTileBits - ls)];
+        for (int r = 0; r < n; r += 2 * half) {
+          const uint64_t u = a[0][r + j], t = mont_mul(a[0][r + j + half], w, p, c);
+          a[0][r + j] = add_mod(u, t, p);
+          a[0][r + j + half] = sub_mod(u, t, p);
+        }
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i) P.data[0][poff + i] = a[0][i];
+}
+
+__global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, uint32_t c) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    a[i] = mont_mul(a[i], f, p, c);
+}
+
+template <int T, int MODE>
+cudaError_t launch_tm(const PassArgs &a, unsigned grid, cudaStream_t st) {
+  constexpr size_t words = ((MODE == kMul ? 2u : 1u) << T) + ((MODE == kMul || MODE == kSqr) ? 2u : 1u) * (1u << (T - 1));
+  constexpr size_t bytes = words * sizeof(uint64_t);
+  if (bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_contig_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(bytes));
+    if (e != cudaSuccess) return e;
+  }
+  ntt_contig_kernel<T, MODE><<<grid, 1 << (T - 4), bytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_mode(const PassArgs &a, unsigned grid, cudaStream_t st) {
+  switch (a.logT) {
+    case 4: return launch_tm<4, MODE>(a, grid, st);
+    case 5: return launch_tm<5, MODE>(a, grid, st);
+    case 6: return launch_tm<6, MODE>(a, grid, st);
+    case 7: return launch_tm<7, MODE>(a, grid, st);
+    case 8: return launch_tm<8, MODE>(a, grid, st);
+    case 9: return launch_tm<9, MODE>(a, grid, st);
+    case 10: return launch_tm<10, MODE>(a, grid, st);
+    case 11: return launch_tm<11, MODE>(a, grid, st);
+    case 12: return launch_tm<12, MODE>(a, grid, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
+  const uint64_t grid = a.tiles * static_cast<uint64_t>(a.nprimes);
+  if (grid == 0 || grid > 0x7fffffffull || a.logS != 0 || a.logR != a.logT) return cudaErrorInvalidValue;
+  const unsigned g = static_cast<unsigned>(grid);
+  if (a.logT < 4) {
+    if (a.logT < 1 || a.logT != a.logN) return cudaErrorInvalidValue;
+    ntt_tiny_kernel<<<g, 1, 0, st>>>(a, mode);
+    return cudaGetLastError();
+  }
+  switch (mode) {
+    case kFwd: return launch_mode<kFwd>(a, g, st);
+    case kInv: return launch_mode<kInv>(a, g, st);
+    case kMul: return launch_mode<kMul>(a, g, st);
+    case kSqr: return launch_mode<kSqr>(a, g, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_scale(uint64_t *a, uint64_t n, uint64_t f, PrimeConst pc, cudaStream_t st) {
+  const int threads = 256;
+  uint64_t blocks = (n + threads - 1) / threads;
+  if (blocks > 152ull * 16) blocks = 152ull * 16;
+  if (blocks == 0) return cudaSuccess;
+  scale_kernel<<<static_cast<unsigned>(blocks), threads, 0, st>>>(a, n, f, pc.p, pc.c);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,125 @@
+// hg_ntt_rounds.cuh -- register rounds shared by the NTT kernels.
+//
+// A CTA owns a tile of 2^T residues (T <= 12).  Tile position x holds row r
+// of column c: strided tiles keep the column in the low bits (x = r << ROWOFF
+// | c), contiguous blocks have ROWOFF = 0.  In a round, each thread holds 16
+// residues whose tile positions differ only in the four bits [A, A+4): the
+// residue of register i sits at xt | (i << A), where xt deposits the thread
+// index into the other bits.  Up to four radix-2 stages run on those
+// registers; between rounds the tile goes through shared memory once.
+//
+// Every shape (A, ROWOFF, which row bits a round owns) is a template
+// argument, so all index arithmetic folds to constants except one thread
+// offset per stage.
+#pragma once
+
+#include "hg_internal.h"
+
+namespace hg {
+namespace rounds {
+
+// Shared-memory word of tile position x: xor bits 4..7 into bits 0..3 so that
+// 16 lanes at a power-of-two stride up to 128 words hit 16 bank pairs.
+__device__ __forceinline__ uint32_t swz(uint32_t x) { return x ^ ((x >> 4) & 15u); }
+
+// Same for the twiddle table, folding bits 4..7 and 8..11.  Linear over xor,
+// so the index of a thread part and a register part can be combined with ^.
+__host__ __device__ __forceinline__ constexpr uint32_t swz_tw(uint32_t e) {
+  return e ^ ((e >> 4) & 15u) ^ ((e >> 8) & 15u);
+}
+
+__device__ __forceinline__ uint32_t bitrev(uint32_t r, int bits) { return __brev(r) >> (32 - bits); }
+
+// Thread part of the tile position for register block [A, A+4).
+template <int A>
+__device__ __forceinline__ uint32_t thread_base(uint32_t tid) {
+  return (tid & ((1u << A) - 1u)) | ((tid >> A) << (A + 4));
+}
+
+// w_R^e, e < R/2, loaded into shared memory at swz_tw(e).
+__device__ __forceinline__ void load_sub_twiddles(uint64_t *tw, const uint64_t *src, int logR, int tid, int nthr) {
+  const int half = 1 << (logR - 1);
+  for (int e = tid; e < half; e += nthr)
+    tw[swz_tw(static_cast<uint32_t>(e))] = __ldg(src + (static_cast<uint64_t>(e) << (kTileBits - logR)));
+}
+
+// Twiddle w_M^E (E < M = 2^logM) in Montgomery form from the two-level tables
+// of w_{2^30}.
+__device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const uint64_t *hi, const uint64_t *lo,
+                                                  uint64_t p, uint32_t c) {
+  const uint64_t e = E << (kLogNmax - logM);
+  const uint64_t th = __ldg(hi + (e >> kTwLevelBits));
+  const uint64_t tl = __ldg(lo + (e & ((1u << kTwLevelBits) - 1)));
+  return mont_mul(th, tl, p, c);
+}
+
+// NB radix-2 stages on register bits [JG, JG+NB) = row bits [BLO, BLO+NB).
+// The stage on row bit b multiplies by w_{2^(b+1)}^(r mod 2^b), read from the
+// R/2-entry table of w_R at (r mod 2^b) << (LOGR-1-b).  r mod 2^b splits into
+// the thread's row bits below b (runtime, zero when TZERO) and the register's
+// (compile time).  With TZERO, butterflies whose twiddle is 1 skip the
+// multiplication.
+template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO>
+__device__ __forceinline__ void stages(uint64_t (&v)[16], const uint64_t *__restrict__ tw, uint32_t xt, uint64_t p,
+                                       uint32_t c) {
+#pragma unroll
+  for (int s = 0; s < NB; ++s) {
+    const int jj = INV ? s : NB - 1 - s;
+    const int j = JG + jj;
+    const int b = BLO + jj;
+    const int sh = LOGR - 1 - b;
+    const uint32_t lowmask = (1u << b) - 1u;
+    const uint32_t ts = TZERO ? 0u : swz_tw(((xt >> ROWOFF) & lowmask) << sh);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (i & (1 << j)) continue;
+      const uint32_t rp = ((static_cast<uint32_t>(i) << A) >> ROWOFF) & lowmask;
+      const bool trivial = TZERO && rp == 0;
+      const uint64_t u = v[i], w = v[i | (1 << j)];
+      if (!INV) {
+        v[i] = add_mod(u, w, p);
+        if (trivial) {
+          v[i | (1 << j)] = sub_mod(u, w, p);
+        } else {
+          const uint64_t t = tw[ts ^ swz_tw(rp << sh)];
+          v[i | (1 << j)] = mont_mul(u - w + p, t, p, c);  // u - w + p in (0, 2p)
+        }
+      } else {
+        const uint64_t t = trivial ? w : mont_mul(w, tw[ts ^ swz_tw(rp << sh)], p, c);
+        v[i] = add_mod(u, t, p);
+        v[i | (1 << j)] = sub_mod(u, t, p);
+      }
+    }
+  }
+}
+
+// Registers <-> shared memory for register block A.
+template <int A>
+__device__ __forceinline__ void to_smem(uint64_t *sm, const uint64_t (&v)[16], uint32_t xt) {
+  const uint32_t sx = swz(xt);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) sm[sx ^ swz(static_cast<uint32_t>(i) << A)] = v[i];
+}
+template <int A>
+__device__ __forceinline__ void from_smem(uint64_t (&v)[16], const uint64_t *sm, uint32_t xt) {
+  const uint32_t sx = swz(xt);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[sx ^ swz(static_cast<uint32_t>(i) << A)];
+}
+
+// Multiply register i by beta * gamma^bitrev4(i) (Montgomery-form beta, gamma):
+// the twiddle w_M^(s * bitrev_R(r)) of the 16 rows r = rhi*16 + i of one
+// column, with beta = w_M^(s * bitrev(rhi)), gamma = w_M^(s * R/16).
+__device__ __forceinline__ void geometric_twiddle(uint64_t (&v)[16], uint64_t beta, uint64_t gamma, uint64_t p,
+                                                  uint32_t c) {
+  uint64_t t = beta;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int i = ((k & 1) << 3) | ((k & 2) << 1) | ((k & 4) >> 1) | ((k & 8) >> 3);  // bitrev4(k)
+    v[i] = mont_mul(v[i], t, p, c);
+    if (k < 15) t = mont_mul(t, gamma, p, c);
+  }
+}
+
+}  // namespace rounds
+}  // namespace hg

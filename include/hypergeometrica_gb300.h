@@ -128,7 +128,8 @@ int hg_ntt_reverse_device(uint64_t *a, size_t n, int mod_num, void *stream);
  * classes index the arrays below. */
 #define HG_KC_NTT_FORWARD 0 /* forward NTT passes (the first also reduces limbs) */
 #define HG_KC_NTT_INVERSE 1 /* inverse NTT passes                               */
-#define HG_KC_POINTWISE 2   /* pointwise product / square                       */
+#define HG_KC_MIDDLE 2      /* last forward pass + pointwise product + first     */
+                            /* inverse pass, fused                               */
 #define HG_KC_CARRY 3       /* reconstruction + carry scan                      */
 #define HG_KC_SMALL 4       /* schoolboy / by-digit products                    */
 #define HG_KC_OTHER 5       /* scaling and other helpers                        */
