@@ -198,9 +198,13 @@ int cuda_fail(cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
 
-constexpr size_t kSubWords = 2048;
+constexpr size_t kSubEntries = 2048;           // (w, companion) pairs per direction
+constexpr size_t kSubWords = 2 * kSubEntries;  // words per direction
 constexpr size_t kLevelWords = size_t(1) << kTwLevelBits;
 constexpr size_t kPrimeTableWords = 2 * kSubWords + 4 * kLevelWords;
+
+// Shoup companion floor(w * 2^64 / p) (calc-b-inv, src/modular-arithmetic.lisp:207-208).
+uint64_t shoup_h(uint64_t w, uint64_t p) { return static_cast<uint64_t>(((u128)w << 64) / p); }
 
 int init_locked(const uint64_t *moduli, int k, int device) {
   Context &c = g_ctx;
@@ -233,9 +237,11 @@ int init_locked(const uint64_t *moduli, int k, int device) {
     uint64_t *sub_f = t, *sub_i = t + kSubWords, *hi_f = t + 2 * kSubWords, *lo_f = hi_f + kLevelWords,
              *hi_i = lo_f + kLevelWords, *lo_i = hi_i + kLevelWords;
     uint64_t a = 1, b = 1;
-    for (size_t e = 0; e < kSubWords; ++e) {
-      sub_f[e] = mont_h(a, p);
-      sub_i[e] = mont_h(b, p);
+    for (size_t e = 0; e < kSubEntries; ++e) {
+      sub_f[2 * e] = a;
+      sub_f[2 * e + 1] = shoup_h(a, p);
+      sub_i[2 * e] = b;
+      sub_i[2 * e + 1] = shoup_h(b, p);
       a = mulmod_h(a, w4096, p);
       b = mulmod_h(b, w4096i, p);
     }
@@ -256,8 +262,8 @@ int init_locked(const uint64_t *moduli, int k, int device) {
   HG_CUDA(cudaMemcpy(c.tables.p, host.data(), host.size() * sizeof(uint64_t), cudaMemcpyHostToDevice), "table upload");
   for (int i = 0; i < kPrimes; ++i) {
     const uint64_t *t = c.tables.u64() + i * kPrimeTableWords;
-    c.tb[i].sub_fwd = t;
-    c.tb[i].sub_inv = t + kSubWords;
+    c.tb[i].sub_fwd = reinterpret_cast<const ulonglong2 *>(t);
+    c.tb[i].sub_inv = reinterpret_cast<const ulonglong2 *>(t + kSubWords);
     c.tb[i].hi_fwd = t + 2 * kSubWords;
     c.tb[i].lo_fwd = c.tb[i].hi_fwd + kLevelWords;
     c.tb[i].hi_inv = c.tb[i].lo_fwd + kLevelWords;
@@ -383,12 +389,13 @@ CrtConst crt_const(int L) {
   const uint64_t R0 = mont_h(1, p0), R1 = mont_h(1, p1), R2 = mont_h(1, p2);  // 2^64 mod p
   const uint64_t inv01 = invmod_h(p0 % p1, p1);
   const uint64_t inv012 = invmod_h(mulmod_h(p0 % p2, p1 % p2, p2), p2);
-  k.k0 = mont_h(mulmod_h(n0, R0, p0), p0);
-  k.k1a = mont_h(mulmod_h(mulmod_h(n1, R1, p1), inv01, p1), p1);
-  k.k1b = mont_h(inv01, p1);
-  k.k2a = mont_h(mulmod_h(mulmod_h(n2, R2, p2), inv012, p2), p2);
-  k.k2b = mont_h(inv012, p2);
-  k.k2c = mont_h(mulmod_h(p0 % p2, inv012, p2), p2);
+  auto pair = [](uint64_t w, uint64_t p) { return make_ulonglong2(w, shoup_h(w, p)); };
+  k.k0 = pair(mulmod_h(n0, R0, p0), p0);
+  k.k1a = pair(mulmod_h(mulmod_h(n1, R1, p1), inv01, p1), p1);
+  k.k1b = pair(inv01, p1);
+  k.k2a = pair(mulmod_h(mulmod_h(n2, R2, p2), inv012, p2), p2);
+  k.k2b = pair(inv012, p2);
+  k.k2c = pair(mulmod_h(p0 % p2, inv012, p2), p2);
   const u128 p01 = (u128)p0 * p1;
   k.p01_lo = static_cast<uint64_t>(p01);
   k.p01_hi = static_cast<uint64_t>(p01 >> 64);

@@ -57,18 +57,49 @@ __device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __
 
 // Montgomery product a * b * 2^-64 mod p, for any 64-bit a and b < p, with
 // p = c * 2^55 + 1.  Result is fully reduced in [0, p).
+//   m = lo * p^-1 mod 2^64 = lo - ((lo * c) mod 2^9) * 2^55   (m1:m0 below)
+//   floor(m * p / 2^64) = u * 2^23 + floor((t mod 2^32) / 2^9) with
+//   t = m0 * c + floor(m / 2^55) and u = m1 * c + floor(t / 2^32) < 2^40;
+// the last product and sum are formed with IMAD (mad.wide.u32), which keeps
+// them off the integer ALU pipe that the butterflies' additions load.
 __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p, uint32_t c) {
   const uint64_t lo = a * b;
   const uint64_t hi = mul_hi64(a, b);  // < p because a < 2^64 and b < p
-  // m = lo * p^-1 mod 2^64 = lo - ((lo * c) mod 2^9) * 2^55
-  const uint32_t lo0 = static_cast<uint32_t>(lo);
-  const uint64_t m = lo - (static_cast<uint64_t>(lo0 * (c << 23)) << 32);
-  // floor(m * p / 2^64) = floor((m * c + floor(m / 2^55)) / 2^9)
-  const uint64_t t = static_cast<uint64_t>(static_cast<uint32_t>(m)) * c + (m >> kShift);
-  const uint64_t u = (m >> 32) * c + (t >> 32);
-  const uint64_t mph = (u << 23) | (static_cast<uint32_t>(t) >> 9);
+  const uint32_t m0 = static_cast<uint32_t>(lo);
+  const uint32_t m1 = static_cast<uint32_t>(lo >> 32) - m0 * (c << 23);
+  uint64_t t;
+  asm("{\n\t.reg .u32 sh;\n\t.reg .u64 shw;\n\t"
+      "shr.u32 sh, %2, 23;\n\t"
+      "cvt.u64.u32 shw, sh;\n\t"
+      "mad.wide.u32 %0, %1, %3, shw;\n\t}"
+      : "=l"(t)
+      : "r"(m0), "r"(m1), "r"(c));
+  const uint64_t u = static_cast<uint64_t>(m1) * c + (t >> 32);
+  uint64_t mph;
+  asm("{\n\t.reg .u32 t9;\n\t.reg .u64 t9w;\n\t"
+      "shr.u32 t9, %1, 9;\n\t"
+      "cvt.u64.u32 t9w, t9;\n\t"
+      "mad.wide.u32 %0, %2, 8388608, t9w;\n\t}"
+      : "=l"(mph)
+      : "r"(static_cast<uint32_t>(t)), "r"(static_cast<uint32_t>(u)));
+  mph += static_cast<uint64_t>(static_cast<uint32_t>(u >> 32)) << 55;
   return fix_neg(hi - mph, p);  // low halves cancel exactly; hi, mph < p
 }
+
+// Shoup product a * w mod p for any 64-bit a, w < p with companion
+// wq = floor(w * 2^64 / p) (the reference's m*/fast2,
+// src/modular-arithmetic.lisp:207-231).  q = floor(a * wq / 2^64) leaves
+// a*w - q*p in [0, 2p); q*p mod 2^64 is q + ((q * c) mod 2^9) * 2^55.
+__device__ __forceinline__ uint64_t shoup_mul(uint64_t a, uint64_t w, uint64_t wq, uint64_t p, uint32_t c) {
+  const uint64_t q = mul_hi64(a, wq);
+  const uint64_t qp = q + (static_cast<uint64_t>(static_cast<uint32_t>(q) * (c << 23)) << 32);
+  return fix_neg(a * w - qp - p, p);
+}
+
+// A twiddle with its Shoup companion.
+struct Tw {
+  uint64_t w, wq;
+};
 
 // x mod p for any 64-bit x (x < 4p because p > 2^62).
 __device__ __forceinline__ uint64_t reduce64(uint64_t x, uint64_t p) {

@@ -72,10 +72,10 @@ struct CrtProducer {
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
-    const uint64_t y0 = mont_mul(r0, k.k0, p0, c0);
-    const uint64_t t1 = sub_mod(mont_mul(r1, k.k1a, p1, c1), mont_mul(y0, k.k1b, p1, c1), p1);
-    uint64_t t2 = sub_mod(mont_mul(r2, k.k2a, p2, c2), mont_mul(y0, k.k2b, p2, c2), p2);
-    t2 = sub_mod(t2, mont_mul(t1, k.k2c, p2, c2), p2);
+    const uint64_t y0 = shoup_mul(r0, k.k0.x, k.k0.y, p0, c0);
+    const uint64_t t1 = sub_mod(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);
+    uint64_t t2 = sub_mod(shoup_mul(r2, k.k2a.x, k.k2a.y, p2, c2), shoup_mul(y0, k.k2b.x, k.k2b.y, p2, c2), p2);
+    t2 = sub_mod(t2, shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
     // V = y0 + p0 t1 + (p0 p1) t2 < p0 p1 p2 < 2^188
     V3 v{y0, 0, 0};
     add128_to(v, p0 * t1, __umul64hi(p0, t1));
@@ -126,34 +126,64 @@ __device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t
   return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | state;
 }
 
-// Carry into the tile from all earlier tiles.  Publishes this tile's
-// aggregate first so that later tiles can proceed.
-__device__ uint32_t look_back(const ScanState &ss, uint64_t tile, GP agg) {
+// Carry into the tile from all earlier tiles, computed by one full warp.
+// Publishes this tile's aggregate first so that later tiles can proceed,
+// then reads the flags of the 32 nearest predecessors at once (lane l reads
+// tile - 1 - l), combines them with a shuffle reduction, and moves to the
+// next window of 32 until some predecessor has published its inclusive
+// carry.  Every lane's wait is bounded; a wait that runs out latches
+// kDevTimeout and the carry is taken as 0.
+__device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, GP agg, int lane) {
   volatile unsigned long long *flags = ss.flags;
   if (tile == 0) return 0;
-  __threadfence();
-  flags[tile] = flag_word(ss.epoch, 1, agg.g, agg.p);
-  GP acc{0, 1};  // identity: carry passes through
-  int64_t j = static_cast<int64_t>(tile) - 1;
-  while (j >= 0) {
-    unsigned long long w;
-    int spins = 0;
-    for (;;) {
-      w = flags[j];
-      if ((w >> 32) == ss.epoch && (w & 3u)) break;
-      if (++spins >= kSpinLimit) {
-        atomicCAS(ss.err, kDevOk, kDevTimeout);
-        return 0;
-      }
-      __nanosleep(64);
-    }
+  if (lane == 0) {
     __threadfence();
-    const uint32_t g = static_cast<uint32_t>((w >> 2) & 1u), p = static_cast<uint32_t>((w >> 3) & 1u);
-    if ((w & 3u) == 2u) return acc.g | (acc.p & g);  // inclusive carry of tile j
-    acc = gp_compose(GP{g, p}, acc);                  // prepend tile j's run
-    --j;
+    flags[tile] = flag_word(ss.epoch, 1, agg.g, agg.p);
   }
-  return acc.g;
+  GP acc{0, 1};  // identity: carry passes through
+  int64_t hi = static_cast<int64_t>(tile) - 1;
+  for (;;) {
+    const int64_t j = hi - lane;
+    GP mine{0, 0};  // before tile 0: a run that emits carry 0
+    bool inclusive = true;
+    bool ok = true;
+    unsigned long long w = 0;
+    if (j >= 0) {
+      int spins = 0;
+      for (;;) {
+        w = flags[j];
+        if ((w >> 32) == ss.epoch && (w & 3u)) break;
+        if (++spins >= kSpinLimit) {
+          ok = false;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    if (__any_sync(0xffffffffu, !ok)) {
+      if (lane == 0) atomicCAS(ss.err, kDevOk, kDevTimeout);
+      return 0;
+    }
+    if (j >= 0) {
+      inclusive = (w & 3u) == 2u;
+      mine = inclusive ? GP{static_cast<uint32_t>((w >> 2) & 1u), 0u}
+                       : GP{static_cast<uint32_t>((w >> 2) & 1u), static_cast<uint32_t>((w >> 3) & 1u)};
+    }
+    const unsigned inc = __ballot_sync(0xffffffffu, inclusive);
+    const int stop = inc ? __ffs(inc) - 1 : 32;  // nearest inclusive lane
+    if (lane > stop) mine = GP{0, 1};
+    // Reduce in significance order: lane 31 least significant, lane 0 most.
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t og = __shfl_down_sync(0xffffffffu, mine.g, d);
+      const uint32_t op = __shfl_down_sync(0xffffffffu, mine.p, d);
+      if (lane + d < 32) mine = gp_compose(GP{og, op}, mine);
+    }
+    const GP win{__shfl_sync(0xffffffffu, mine.g, 0), __shfl_sync(0xffffffffu, mine.p, 0)};
+    acc = gp_compose(win, acc);
+    if (inc) return acc.g;
+    hi -= 32;
+  }
 }
 
 template <class Producer>
@@ -243,16 +273,18 @@ __global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer pro
     excl = lane == 0 ? GP{0, 1} : GP{og, op};
   }
   excl = gp_compose(wpre, excl);  // runs over positions before this thread, within the tile
-  if (tid == 0) {
+  if (wid == 0) {
     GP agg{0, 1};
     for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
-    const uint32_t cin = look_back(ss, tile, agg);
-    const uint32_t cout = agg.g | (agg.p & cin);
-    __threadfence();
-    reinterpret_cast<volatile unsigned long long *>(ss.flags)[tile] = flag_word(ss.epoch, 2, cout, 0);
-    s_cin = cin;
-    const uint64_t last = tile * kCarryTile + kCarryTile;
-    if (last >= nproc && tile * kCarryTile < nproc && cout) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
+    const uint32_t cin = look_back_warp(ss, tile, agg, lane);
+    if (lane == 0) {
+      const uint32_t cout = agg.g | (agg.p & cin);
+      __threadfence();
+      reinterpret_cast<volatile unsigned long long *>(ss.flags)[tile] = flag_word(ss.epoch, 2, cout, 0);
+      s_cin = cin;
+      const uint64_t last = tile * kCarryTile + kCarryTile;
+      if (last >= nproc && tile * kCarryTile < nproc && cout) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
+    }
   }
   __syncthreads();
   uint32_t cin = excl.g | (excl.p & s_cin);

@@ -11,8 +11,8 @@ namespace hg {
 
 // Device twiddle tables of one prime, all in Montgomery form.
 struct NttTables {
-  const uint64_t *sub_fwd;  // w_4096^e, e < 2048     (sub-transform twiddles, any R <= 4096)
-  const uint64_t *sub_inv;  // w_4096^-e
+  const ulonglong2 *sub_fwd;  // (w_4096^e, Shoup companion), e < 2048: sub-transform twiddles, any R <= 4096
+  const ulonglong2 *sub_inv;  // (w_4096^-e, companion)
   const uint64_t *hi_fwd;   // w_{2^30}^(e * 2^15), e < 2^15
   const uint64_t *lo_fwd;   // w_{2^30}^e,          e < 2^15
   const uint64_t *hi_inv;
@@ -41,12 +41,13 @@ struct PassArgs {
 };
 
 // Constants of the Garner reconstruction for one transform length.
+// Each constant is a (value, Shoup companion) pair.
 struct CrtConst {
   PrimeConst pc[kPrimes];
-  uint64_t k0;             // Mont(N^-1 * 2^64)                    mod p0
-  uint64_t k1a, k1b;       // Mont(N^-1 2^64 p0^-1), Mont(p0^-1)    mod p1
-  uint64_t k2a, k2b, k2c;  // Mont(N^-1 2^64 (p0p1)^-1), Mont((p0p1)^-1), Mont(p1^-1) mod p2
-  uint64_t p01_lo, p01_hi; // p0 * p1
+  ulonglong2 k0;            // N^-1 2^64                                         mod p0
+  ulonglong2 k1a, k1b;      // N^-1 2^64 p0^-1, p0^-1                            mod p1
+  ulonglong2 k2a, k2b, k2c; // N^-1 2^64 (p0p1)^-1, (p0p1)^-1, p1^-1            mod p2
+  uint64_t p01_lo, p01_hi;  // p0 * p1
 };
 
 // Carry-scan launch state (decoupled look-back across tiles).

@@ -42,7 +42,7 @@ struct Groups {
 };
 
 template <int T, int g, bool INV>
-__device__ __forceinline__ void round_g(uint64_t (&v)[16], const uint64_t *tw, uint32_t xt, uint64_t p, uint32_t c) {
+__device__ __forceinline__ void round_g(uint64_t (&v)[16], const ulonglong2 *tw, uint32_t xt, uint64_t p, uint32_t c) {
   using Gr = Groups<T>;
   constexpr int A = Gr::template A<g>();
   constexpr int NB = Gr::template NB<g>();
@@ -67,7 +67,7 @@ __device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_
 
 // All forward rounds, from the top group down to group 0.
 template <int T>
-__device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, const uint64_t *tw, uint32_t &xt,
+__device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
   if constexpr (G == 3) {
@@ -87,7 +87,7 @@ __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, 
 
 // All inverse rounds, from group 0 up to the top group.
 template <int T>
-__device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const uint64_t *tw, uint32_t &xt,
+__device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
   round_g<T, 0, true>(v, tw, xt, p, c);
@@ -140,13 +140,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
   const uint64_t base = tile << T;
 
   constexpr bool TWO = (MODE == kMul);
-  constexpr bool NEED_F = (MODE != kInv), NEED_I = (MODE != kFwd);
   uint64_t *smA = smem;
   uint64_t *smB = smem + (TWO ? (1u << T) : 0u);
-  uint64_t *twf = smem + ((TWO ? 2u : 1u) << T);
-  uint64_t *twi = twf + (NEED_F ? HALF : 0u);
-  if (NEED_F) load_sub_twiddles(twf, tb.sub_fwd, T, tid, NTHR);
-  if (NEED_I) load_sub_twiddles(twi, tb.sub_inv, T, tid, NTHR);
+  // One table of (twiddle, companion) pairs: the forward one, replaced by
+  // the inverse one after the pointwise product.
+  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) << T));
+  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, NTHR);
 
   uint64_t v[16];
   uint32_t xt;
@@ -154,14 +153,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
     xt = thread_base<A0>(tid);
     load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
     __syncthreads();
-    inverse_rounds<T>(v, smA, twi, xt, tid, p, c);
+    inverse_rounds<T>(v, smA, tw, xt, tid, p, c);
     store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
   } else {
     xt = thread_base<ATOP>(tid);
     load_block<ATOP>(v, P.data[0] + poff, P.limbs[0], P.nlimbs[0], base, xt, p);
     __syncthreads();
-    forward_rounds<T>(v, smA, twf, xt, tid, p, c);
+    forward_rounds<T>(v, smA, tw, xt, tid, p, c);
     if constexpr (MODE == kFwd) {
       store_block<A0>(v, P.data[0] + poff, base, xt);
       return;
@@ -173,7 +172,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
         to_smem<A0>(smA, v, xt);
         uint32_t xb = thread_base<ATOP>(tid);
         load_block<ATOP>(v, P.data[1] + poff, P.limbs[1], P.nlimbs[1], base, xb, p);
-        forward_rounds<T>(v, smB, twf, xb, tid, p, c);
+        forward_rounds<T>(v, smB, tw, xb, tid, p, c);
         const uint32_t sx = swz(xb);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(smA[sx ^ swz(static_cast<uint32_t>(i) << A0)], v[i], p, c);
@@ -183,7 +182,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
-      inverse_rounds<T>(v, smA, twi, xt, tid, p, c);
+      __syncthreads();  // every thread is done with the forward table
+      load_sub_twiddles(tw, tb.sub_inv, T, tid, NTHR);
+      __syncthreads();
+      inverse_rounds<T>(v, smA, tw, xt, tid, p, c);
       store_block<ATOP>(v, P.data[0] + poff, base, xt);
     }
   }
@@ -209,11 +211,11 @@ __global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
       for (int ls = L; ls >= 1; --ls) {  // DIF, subn = 2^ls
         const int half = 1 << (ls - 1);
         for (int j = 0; j < half; ++j) {
-          const uint64_t w = tb.sub_fwd[static_cast<uint64_t>(j) << (kTileBits - ls)];
+          const ulonglong2 w = tb.sub_fwd[static_cast<uint64_t>(j) << (kTileBits - ls)];
           for (int r = 0; r < n; r += 2 * half) {
             const uint64_t u = a[op][r + j], x = a[op][r + j + half];
             a[op][r + j] = add_mod(u, x, p);
-            a[op][r + j + half] = mont_mul(u - x + p, w, p, c);
+            a[op][r + j + half] = shoup_mul(u - x + p, w.x, w.y, p, c);
           }
         }
       }
@@ -224,9 +226,9 @@ __global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
     for (int ls = 1; ls <= L; ++ls) {  // DIT, subn = 2^ls
       const int half = 1 << (ls - 1);
       for (int j = 0; j < half; ++j) {
-        const uint64_t w = tb.sub_inv[static_cast<uint64_t>(j) << (kTileBits - ls)];
+        const ulonglong2 w = tb.sub_inv[static_cast<uint64_t>(j) << (kTileBits - ls)];
         for (int r = 0; r < n; r += 2 * half) {
-          const uint64_t u = a[0][r + j], t = mont_mul(a[0][r + j + half], w, p, c);
+          const uint64_t u = a[0][r + j], t = shoup_mul(a[0][r + j + half], w.x, w.y, p, c);
           a[0][r + j] = add_mod(u, t, p);
           a[0][r + j + half] = sub_mod(u, t, p);
         }
@@ -244,8 +246,7 @@ __global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, ui
 
 template <int T, int MODE>
 cudaError_t launch_tm(const PassArgs &a, unsigned grid, cudaStream_t st) {
-  constexpr size_t words = ((MODE == kMul ? 2u : 1u) << T) + ((MODE == kMul || MODE == kSqr) ? 2u : 1u) * (1u << (T - 1));
-  constexpr size_t bytes = words * sizeof(uint64_t);
+  constexpr size_t bytes = ((MODE == kMul ? 2u : 1u) << T) * sizeof(uint64_t) + (1u << (T - 1)) * sizeof(ulonglong2);
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(ntt_contig_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(bytes));

@@ -22,10 +22,13 @@ namespace rounds {
 // 16 lanes at a power-of-two stride up to 128 words hit 16 bank pairs.
 __device__ __forceinline__ uint32_t swz(uint32_t x) { return x ^ ((x >> 4) & 15u); }
 
-// Same for the twiddle table, folding bits 4..7 and 8..11.  Linear over xor,
-// so the index of a thread part and a register part can be combined with ^.
+// Index of twiddle e in the shared table of 16-byte (w, wq) pairs: xor bits
+// 3..5, 6..8 and 9..11 into bits 0..2, so that the 8 lanes a 16-byte access
+// serves together, reading entries at a power-of-two stride, hit 8
+// different bank quads.  Linear over xor, so the index of a thread part and
+// a register part can be combined with ^.
 __host__ __device__ __forceinline__ constexpr uint32_t swz_tw(uint32_t e) {
-  return e ^ ((e >> 4) & 15u) ^ ((e >> 8) & 15u);
+  return e ^ ((e >> 3) & 7u) ^ ((e >> 6) & 7u) ^ ((e >> 9) & 7u);
 }
 
 __device__ __forceinline__ uint32_t bitrev(uint32_t r, int bits) { return __brev(r) >> (32 - bits); }
@@ -36,8 +39,8 @@ __device__ __forceinline__ uint32_t thread_base(uint32_t tid) {
   return (tid & ((1u << A) - 1u)) | ((tid >> A) << (A + 4));
 }
 
-// w_R^e, e < R/2, loaded into shared memory at swz_tw(e).
-__device__ __forceinline__ void load_sub_twiddles(uint64_t *tw, const uint64_t *src, int logR, int tid, int nthr) {
+// (w_R^e, companion), e < R/2, loaded into shared memory at swz_tw(e).
+__device__ __forceinline__ void load_sub_twiddles(ulonglong2 *tw, const ulonglong2 *src, int logR, int tid, int nthr) {
   const int half = 1 << (logR - 1);
   for (int e = tid; e < half; e += nthr)
     tw[swz_tw(static_cast<uint32_t>(e))] = __ldg(src + (static_cast<uint64_t>(e) << (kTileBits - logR)));
@@ -60,7 +63,7 @@ __device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const ui
 // (compile time).  With TZERO, butterflies whose twiddle is 1 skip the
 // multiplication.
 template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO>
-__device__ __forceinline__ void stages(uint64_t (&v)[16], const uint64_t *__restrict__ tw, uint32_t xt, uint64_t p,
+__device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__restrict__ tw, uint32_t xt, uint64_t p,
                                        uint32_t c) {
 #pragma unroll
   for (int s = 0; s < NB; ++s) {
@@ -81,11 +84,15 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const uint64_t *__rest
         if (trivial) {
           v[i | (1 << j)] = sub_mod(u, w, p);
         } else {
-          const uint64_t t = tw[ts ^ swz_tw(rp << sh)];
-          v[i | (1 << j)] = mont_mul(u - w + p, t, p, c);  // u - w + p in (0, 2p)
+          const ulonglong2 t = tw[ts ^ swz_tw(rp << sh)];
+          v[i | (1 << j)] = shoup_mul(u - w + p, t.x, t.y, p, c);  // u - w + p in (0, 2p)
         }
       } else {
-        const uint64_t t = trivial ? w : mont_mul(w, tw[ts ^ swz_tw(rp << sh)], p, c);
+        uint64_t t = w;
+        if (!trivial) {
+          const ulonglong2 tt = tw[ts ^ swz_tw(rp << sh)];
+          t = shoup_mul(w, tt.x, tt.y, p, c);
+        }
         v[i] = add_mod(u, t, p);
         v[i | (1 << j)] = sub_mod(u, t, p);
       }

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
   constexpr int G = (LOGR + 3) / 4;
   constexpr int NB1 = LOGR - 4;  // row bits of the top group (when G == 2)
   static_assert(LOGR >= 4 && LOGR <= 8, "strided passes have 4..8 row bits");
-  __shared__ uint64_t tw[1 << (LOGR - 1)];
+  __shared__ ulonglong2 tw[1 << (LOGR - 1)];
   __shared__ uint64_t sm[G == 2 ? (1 << T) : 1];
 
   const uint32_t tid = threadIdx.x;
