@@ -48,6 +48,15 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 _sz = ctypes.c_size_t
 _vp = ctypes.c_void_p
 
+
+class HgProduct(ctypes.Structure):
+    """hg_product: one product of a batch (device pointers; y NULL squares x)."""
+
+    _fields_ = [("x", _vp), ("nx", _sz), ("y", _vp), ("ny", _sz), ("out", _vp), ("nout", _sz)]
+
+
+HG_BATCH_AUTOTUNE = 1
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "hg_init": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int]),
@@ -65,6 +74,10 @@ SIGNATURES = {
     "hg_sqr_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp]),
     "hg_mul_schoolboy_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
     "hg_sync": (ctypes.c_int, [_vp]),
+    "hg_batch_create": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "hg_batch_run": (ctypes.c_int, [_vp, _vp]),
+    "hg_batch_destroy": (ctypes.c_int, [_vp]),
+    "hg_mul_batch_device": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, _vp]),
     "hg_ntt_forward_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
     "hg_ntt_reverse_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
     "hg_profile_enable": (ctypes.c_int, [ctypes.c_int]),

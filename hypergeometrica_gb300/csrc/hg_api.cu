@@ -11,8 +11,11 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "hg_internal.h"
@@ -330,6 +333,8 @@ PassArgs base_args(int L, int nops) {
   a.prime_lo = 0;
   a.nprimes = kPrimes;
   a.prime_stride = uint64_t(1) << L;
+  a.nprod = 1;
+  a.ws_stride = static_cast<uint64_t>(kPrimes) << L;
   for (int i = 0; i < kPrimes; ++i) {
     a.pc[i] = g_ctx.pc[i];
     a.tb[i] = g_ctx.tb[i];
@@ -364,6 +369,7 @@ cudaError_t run_strided(PassArgs a, const std::vector<PassPlan> &plan, bool inve
     }
     if (e != cudaSuccess) return e;
     a.limbs[0] = a.limbs[1] = nullptr;  // only the first forward pass reads limbs
+    a.read_limbs = 0;
   }
   return cudaSuccess;
 }
@@ -536,6 +542,19 @@ int read_device_error(cudaStream_t st) {
   return HG_OK;
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc, pinned torch
+// tensors, cudaHostRegister), or nullptr for pageable or unknown memory.
+const void *pinned_view(const void *h) {
+  if (!h) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unregistered pointer
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 // Host-memory wrapper: stage operands, run, copy back, check.
 enum class Kind { Ntt, Square, Schoolboy, Digit };
 
@@ -562,21 +581,36 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
   }
   const size_t nd = size;  // limbs computed on the device; the rest are zero
   cudaStream_t st = c.stream;
-  HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
-  HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
-  if (kind == Kind::Ntt || kind == Kind::Schoolboy) {
+  // Pinned (page-locked) host buffers are addressable from the device over
+  // the host link, so the kernels read the operands and write the product
+  // in place; pageable buffers go through device staging buffers.
+  const bool two = (kind == Kind::Ntt || kind == Kind::Schoolboy);
+  const uint64_t *dx = static_cast<const uint64_t *>(pinned_view(x));
+  const uint64_t *dy = two ? static_cast<const uint64_t *>(pinned_view(y)) : nullptr;
+  uint64_t *dout = static_cast<uint64_t *>(const_cast<void *>(pinned_view(out)));
+  if (!dx) {
+    HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
+    HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
+    dx = c.X.u64();
+  }
+  if (two && !dy) {
     HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
     HG_CUDA(cudaMemcpyAsync(c.Y.p, y, ny * 8, cudaMemcpyHostToDevice, st), "operand upload");
+    dy = c.Y.u64();
   }
-  HG_CUDA(c.OUT.ensure(nd * 8), "result allocation");
+  const bool staged_out = (dout == nullptr);
+  if (staged_out) {
+    HG_CUDA(c.OUT.ensure(nd * 8), "result allocation");
+    dout = c.OUT.u64();
+  }
   switch (kind) {
-    case Kind::Ntt: rc = ntt_product_device(c.X.u64(), nx, c.Y.u64(), ny, c.OUT.u64(), nd, st); break;
-    case Kind::Square: rc = ntt_product_device(c.X.u64(), nx, nullptr, 0, c.OUT.u64(), nd, st); break;
-    case Kind::Schoolboy: rc = small_product_device(c.X.u64(), nx, c.Y.u64(), ny, 0, c.OUT.u64(), nd, st); break;
-    case Kind::Digit: rc = small_product_device(c.X.u64(), nx, nullptr, 0, d, c.OUT.u64(), nd, st); break;
+    case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st); break;
+    case Kind::Square: rc = ntt_product_device(dx, nx, nullptr, 0, dout, nd, st); break;
+    case Kind::Schoolboy: rc = small_product_device(dx, nx, dy, ny, 0, dout, nd, st); break;
+    case Kind::Digit: rc = small_product_device(dx, nx, nullptr, 0, d, dout, nd, st); break;
   }
   if (rc) return rc;
-  HG_CUDA(cudaMemcpyAsync(out, c.OUT.p, nd * 8, cudaMemcpyDeviceToHost, st), "result download");
+  if (staged_out) HG_CUDA(cudaMemcpyAsync(out, dout, nd * 8, cudaMemcpyDeviceToHost, st), "result download");
   rc = read_device_error(st);
   if (rc) return rc;
   if (nout > nd) memset(out + nd, 0, (nout - nd) * sizeof(uint64_t));
@@ -615,12 +649,305 @@ int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) 
   return HG_OK;
 }
 
+// ---- batches -------------------------------------------------------------
+
+// Products of one transform length (and kind) run by one launch per pass.
+struct BatchGroup {
+  int L = 0;
+  bool square = false;
+  bool tails = false;              // some product has nout > N
+  std::vector<PassPlan> plan;
+  uint64_t first = 0, nprod = 0;   // descriptors [first, first + nprod)
+  uint64_t flags_off = 0;          // first carry-scan flag word
+};
+
+// Candidate pass splits of a 2^L transform: the default plan and, for
+// L >= 12, every contiguous block size T with the remaining L - T bits in
+// as few strided passes of 4..8 bits as possible.
+std::vector<std::vector<PassPlan>> plan_candidates(int L) {
+  std::vector<std::vector<PassPlan>> out{plan_passes(L)};
+  if (L < kTileBits) return out;
+  for (int T = 4; T <= kTileBits; ++T) {
+    const int rem = L - T;
+    if (rem < 4) continue;
+    const int k = (rem + 7) / 8;
+    if (rem < 4 * k) continue;
+    std::vector<PassPlan> v;
+    int logS = L;
+    for (int i = 0; i < k; ++i) {
+      const int part = rem / k + (i < rem % k ? 1 : 0);
+      logS -= part;
+      v.push_back({part, logS, kTileBits});
+    }
+    // A strided pass over R rows needs columns of at least 2^(12 - logR)
+    // words so that its 4096-word tile spans whole rows.
+    if (logS + v.back().logR < kTileBits) continue;
+    v.push_back({logS, 0, logS});
+    bool same = v.size() == out[0].size();
+    for (size_t i = 0; same && i < v.size(); ++i)
+      same = v[i].logR == out[0][i].logR && v[i].logS == out[0][i].logS && v[i].logT == out[0][i].logT;
+    if (!same) out.push_back(v);
+  }
+  return out;
+}
+
+// Schedules chosen by timing, keyed by (L, square, products in the group).
+std::mutex g_tune_mu;
+std::map<std::tuple<int, bool, uint64_t>, std::vector<PassPlan>> g_tuned;
+
+}  // namespace
+}  // namespace hg
+
+struct hg_batch {
+  std::vector<hg::BatchGroup> groups;
+  std::vector<hg::ProductDesc> desc;  // groups contiguous, then the zero products
+  uint64_t zero_first = 0, nzero = 0;
+  uint64_t ws_words = 0, flag_words = 0;
+  hg::DevBuf d_desc, ws, flags, tickets;
+};
+
+namespace hg {
+namespace {
+
+// Enqueue one group with the given schedule.  The group's ticket and flags
+// must be zero.
+int run_group(hg_batch *b, size_t gi, const std::vector<PassPlan> &plan, cudaStream_t st) {
+  const BatchGroup &g = b->groups[gi];
+  const int nops = g.square ? 1 : 2;
+  const uint64_t N = uint64_t(1) << g.L;
+  const uint64_t slab = static_cast<uint64_t>(kPrimes) * N;
+  const ProductDesc *d = static_cast<const ProductDesc *>(b->d_desc.p) + g.first;
+  uint64_t *ws = b->ws.u64();
+  if (g.tails) HG_CUDA(launch_zero_tails(d, g.nprod, N, st), "zero tails");
+  PassArgs a = base_args(g.L, nops);
+  a.batch = d;
+  a.read_limbs = 1;
+  a.nprod = g.nprod;
+  a.ws_stride = slab;
+  a.data[0] = ws;
+  a.data[1] = ws + g.nprod * slab;
+  HG_CUDA(run_strided(a, plan, false, st), "forward transform");
+  PassArgs m = a;
+  if (plan.size() > 1) m.read_limbs = 0;
+  HG_CUDA(run_contig(m, plan.back(), g.square ? kContigSqr : kContigMul, st), "middle pass");
+  PassArgs inv = base_args(g.L, 1);
+  inv.batch = d;
+  inv.nprod = g.nprod;
+  inv.ws_stride = slab;
+  inv.data[0] = ws;
+  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
+  ScanState ss;
+  ss.ticket = static_cast<unsigned long long *>(b->tickets.p) + gi;
+  ss.ticket_base = 0;
+  ss.flags = static_cast<unsigned long long *>(b->flags.p) + g.flags_off;
+  ss.epoch = 1;
+  ss.err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
+  {
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(N) * static_cast<double>(g.nprod));
+    HG_CUDA(launch_crt_carry_batch(ws, slab, g.L, crt_const(g.L), d, g.nprod, ss, st), "reconstruction");
+  }
+  return HG_OK;
+}
+
+int batch_clear_scan(hg_batch *b, cudaStream_t st) {
+  if (b->flag_words) HG_CUDA(cudaMemsetAsync(b->flags.p, 0, b->flag_words * 8, st), "scan flags reset");
+  if (!b->groups.empty())
+    HG_CUDA(cudaMemsetAsync(b->tickets.p, 0, b->groups.size() * 8, st), "scan tickets reset");
+  return HG_OK;
+}
+
+// Time each candidate schedule of each group (twice; the second run counts)
+// and keep the fastest.
+int batch_autotune(hg_batch *b) {
+  cudaStream_t st = g_ctx.stream;
+  cudaEvent_t e0, e1;
+  HG_CUDA(cudaEventCreate(&e0), "event creation");
+  HG_CUDA(cudaEventCreate(&e1), "event creation");
+  int rc = HG_OK;
+  for (size_t gi = 0; gi < b->groups.size() && rc == HG_OK; ++gi) {
+    BatchGroup &g = b->groups[gi];
+    const auto key = std::make_tuple(g.L, g.square, g.nprod);
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tuned.find(key);
+      if (it != g_tuned.end()) {
+        g.plan = it->second;
+        continue;
+      }
+    }
+    const auto cands = plan_candidates(g.L);
+    float best = 1e30f;
+    for (const auto &plan : cands) {
+      float ms = 0;
+      for (int rep = 0; rep < 2 && rc == HG_OK; ++rep) {
+        if ((rc = batch_clear_scan(b, st))) break;
+        cudaEventRecord(e0, st);
+        if ((rc = run_group(b, gi, plan, st))) break;
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(HG_ERR_CUDA, "autotune timing failed");
+        else cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (rc) break;
+      if (ms < best) {
+        best = ms;
+        g.plan = plan;
+      }
+    }
+    if (rc == HG_OK) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tuned[key] = g.plan;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == HG_OK) rc = read_device_error(st);
+  return rc;
+}
+
+constexpr uint64_t kBatchWorkspaceCap = uint64_t(4) << 30;  // bytes per group chunk
+
+int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
+  if (!out || (n && !prods)) return fail(HG_ERR_ARG, "null pointer");
+  *out = nullptr;
+  std::unique_ptr<hg_batch> b(new hg_batch());
+  struct Item {
+    int L;
+    bool square;
+    size_t i;
+  };
+  std::vector<Item> items, zeros;
+  for (size_t i = 0; i < n; ++i) {
+    const hg_product &p = prods[i];
+    const bool square = p.y == nullptr;
+    const uint64_t size = square ? 2 * p.nx : p.nx + p.ny;
+    if (!p.out || (p.nx && !p.x)) return fail(HG_ERR_ARG, "product %zu: null pointer", i);
+    if (p.nout < size) return fail(HG_ERR_ARG, "product %zu: nout = %zu cannot hold %llu limbs", i, p.nout,
+                                   (unsigned long long)size);
+    if (p.nx == 0 || (!square && p.ny == 0)) {
+      zeros.push_back({0, square, i});
+      continue;
+    }
+    const int L = ilog2_ceil(size);
+    int rc = check_len(L);
+    if (rc) return rc;
+    items.push_back({L, square, i});
+  }
+  std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &c) {
+    return a.L != c.L ? a.L < c.L : a.square < c.square;
+  });
+  auto desc_of = [&](size_t i) {
+    const hg_product &p = prods[i];
+    return ProductDesc{p.x, p.y, p.nx, p.y ? p.ny : p.nx, p.out, p.nout};
+  };
+  for (size_t s = 0; s < items.size();) {
+    size_t e = s;
+    while (e < items.size() && items[e].L == items[s].L && items[e].square == items[s].square) ++e;
+    const int L = items[s].L;
+    const bool square = items[s].square;
+    const uint64_t N = uint64_t(1) << L;
+    const uint64_t per = static_cast<uint64_t>(square ? 1 : 2) * kPrimes * N * 8;  // workspace bytes per product
+    const uint64_t chunk = std::max<uint64_t>(1, kBatchWorkspaceCap / per);
+    for (size_t c = s; c < e; c += chunk) {
+      BatchGroup g;
+      g.L = L;
+      g.square = square;
+      g.plan = plan_passes(L);
+      g.first = b->desc.size();
+      g.nprod = std::min<uint64_t>(chunk, e - c);
+      g.flags_off = b->flag_words;
+      for (size_t k = c; k < c + g.nprod; ++k) {
+        b->desc.push_back(desc_of(items[k].i));
+        if (b->desc.back().nout > N) g.tails = true;
+      }
+      b->flag_words += carry_tiles(N) * g.nprod;
+      b->ws_words = std::max<uint64_t>(b->ws_words, per / 8 * g.nprod);
+      b->groups.push_back(g);
+    }
+    s = e;
+  }
+  b->zero_first = b->desc.size();
+  b->nzero = zeros.size();
+  for (const Item &z : zeros) b->desc.push_back(desc_of(z.i));
+  Context &c = g_ctx;
+  if (!b->desc.empty()) {
+    HG_CUDA(b->d_desc.ensure(b->desc.size() * sizeof(ProductDesc)), "batch descriptors");
+    HG_CUDA(cudaMemcpy(b->d_desc.p, b->desc.data(), b->desc.size() * sizeof(ProductDesc), cudaMemcpyHostToDevice),
+            "batch descriptors upload");
+  }
+  if (b->ws_words) HG_CUDA(b->ws.ensure(b->ws_words * 8), "batch workspace");
+  if (b->flag_words) HG_CUDA(b->flags.ensure(b->flag_words * 8), "batch scan flags");
+  HG_CUDA(b->tickets.ensure(std::max<size_t>(1, b->groups.size()) * 8), "batch tickets");
+  (void)c;
+  if (flags & HG_BATCH_AUTOTUNE) {
+    int rc = batch_autotune(b.get());
+    if (rc) return rc;
+  } else {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (BatchGroup &g : b->groups) {
+      auto it = g_tuned.find(std::make_tuple(g.L, g.square, g.nprod));
+      if (it != g_tuned.end()) g.plan = it->second;
+    }
+  }
+  *out = b.release();
+  return HG_OK;
+}
+
+int batch_run(hg_batch *b, cudaStream_t st) {
+  if (!b) return fail(HG_ERR_ARG, "null batch");
+  int rc = batch_clear_scan(b, st);
+  if (rc) return rc;
+  if (b->nzero)
+    HG_CUDA(launch_zero_tails(static_cast<const ProductDesc *>(b->d_desc.p) + b->zero_first, b->nzero, 0, st),
+            "zero products");
+  for (size_t gi = 0; gi < b->groups.size(); ++gi)
+    if ((rc = run_group(b, gi, b->groups[gi].plan, st))) return rc;
+  return HG_OK;
+}
+
 }  // namespace
 }  // namespace hg
 
 using namespace hg;
 
 extern "C" {
+
+int hg_batch_create(const hg_product *prods, size_t n, int flags, hg_batch **batch) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  return batch_create(prods, n, flags, batch);
+}
+
+int hg_batch_run(hg_batch *batch, void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  return batch_run(batch, static_cast<cudaStream_t>(stream));
+}
+
+int hg_batch_destroy(hg_batch *batch) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  if (!batch) return HG_OK;
+  batch->d_desc.release();
+  batch->ws.release();
+  batch->flags.release();
+  batch->tickets.release();
+  delete batch;
+  return HG_OK;
+}
+
+int hg_mul_batch_device(const hg_product *prods, size_t n, void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  hg_batch *b = nullptr;
+  if ((rc = batch_create(prods, n, 0, &b))) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = batch_run(b, st);
+  if (rc == HG_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(HG_ERR_CUDA, "stream synchronise failed");
+  hg_batch_destroy(b);
+  return rc;
+}
 
 int hg_init(const uint64_t *moduli, int k, int device) {
   std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);

@@ -45,15 +45,19 @@ struct CrtProducer {
   uint64_t n;           // N
   CrtConst k;
 
-  __device__ __forceinline__ V3 operator()(uint64_t i) const { return garner(res[i], res[n + i], res[2 * n + i]); }
+  // Coefficient i of the product whose residues start `off` words past res.
+  __device__ __forceinline__ V3 at(uint64_t off, uint64_t i) const {
+    const uint64_t *r = res + off;
+    return garner(r[i], r[n + i], r[2 * n + i]);
+  }
 
   // Eight consecutive positions from i0 (a multiple of 8): 16-byte loads.
-  __device__ __forceinline__ void eight(uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+  __device__ __forceinline__ void eight(uint64_t off, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
     if (i0 + 8 <= nproc) {
       uint64_t r[3][8];
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(res + j * n + i0);
+        const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(res + off + j * n + i0);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const ulonglong2 w = __ldg(src + q);
@@ -65,7 +69,7 @@ struct CrtProducer {
       for (int k8 = 0; k8 < 8; ++k8) v[k8] = garner(r[0][k8], r[1][k8], r[2][k8]);
     } else {
 #pragma unroll
-      for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? (*this)(i0 + k8) : V3{0, 0, 0};
+      for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? at(off, i0 + k8) : V3{0, 0, 0};
     }
   }
 
@@ -97,12 +101,12 @@ struct ConvProducer {
   uint64_t ny;
   uint64_t dval;
 
-  __device__ __forceinline__ void eight(uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+  __device__ __forceinline__ void eight(uint64_t, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
 #pragma unroll
-    for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? (*this)(i0 + k8) : V3{0, 0, 0};
+    for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? at(0, i0 + k8) : V3{0, 0, 0};
   }
 
-  __device__ __forceinline__ V3 operator()(uint64_t i) const {
+  __device__ __forceinline__ V3 at(uint64_t, uint64_t i) const {
     V3 v{0, 0, 0};
     if (!y) {
       if (i < nx) {
@@ -133,22 +137,23 @@ __device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t
 // next window of 32 until some predecessor has published its inclusive
 // carry.  Every lane's wait is bounded; a wait that runs out latches
 // kDevTimeout and the carry is taken as 0.
-__device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, GP agg, int lane) {
+__device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, uint64_t first, GP agg, int lane) {
   volatile unsigned long long *flags = ss.flags;
-  if (tile == 0) return 0;
+  if (tile == first) return 0;  // the product's first tile
   if (lane == 0) {
     __threadfence();
     flags[tile] = flag_word(ss.epoch, 1, agg.g, agg.p);
   }
   GP acc{0, 1};  // identity: carry passes through
   int64_t hi = static_cast<int64_t>(tile) - 1;
+  const int64_t lo = static_cast<int64_t>(first);
   for (;;) {
     const int64_t j = hi - lane;
-    GP mine{0, 0};  // before tile 0: a run that emits carry 0
+    GP mine{0, 0};  // before the product's first tile: a run that emits carry 0
     bool inclusive = true;
     bool ok = true;
     unsigned long long w = 0;
-    if (j >= 0) {
+    if (j >= lo) {
       int spins = 0;
       for (;;) {
         w = flags[j];
@@ -164,7 +169,7 @@ __device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, GP agg, i
       if (lane == 0) atomicCAS(ss.err, kDevOk, kDevTimeout);
       return 0;
     }
-    if (j >= 0) {
+    if (j >= lo) {
       inclusive = (w & 3u) == 2u;
       mine = inclusive ? GP{static_cast<uint32_t>((w >> 2) & 1u), 0u}
                        : GP{static_cast<uint32_t>((w >> 2) & 1u), static_cast<uint32_t>((w >> 3) & 1u)};
@@ -186,9 +191,14 @@ __device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, GP agg, i
   }
 }
 
+// One tile of 2048 output limbs per CTA.  Single product: tiles in ticket
+// order.  Batch (batch != nullptr): tickets run product-major, tpp tiles per
+// product; product k's residues are rebased by k * ws_stride, its output is
+// batch[k].out[0, min(nout, n)), and the look-back stops at its first tile.
 template <class Producer>
-__global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer prod, uint64_t *__restrict__ out,
-                                                              uint64_t nproc, ScanState ss) {
+__global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer prod0, uint64_t *__restrict__ out,
+                                                              uint64_t nproc, ScanState ss, const ProductDesc *batch,
+                                                              uint64_t tpp, uint64_t ws_stride, uint64_t n) {
   __shared__ uint64_t s_prev[kCarryThreads][9];
   __shared__ GP s_warp[kCarryThreads / 32];
   __shared__ unsigned long long s_tile;
@@ -197,23 +207,35 @@ __global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer pro
 
   if (tid == 0) s_tile = atomicAdd(ss.ticket, 1ull) - ss.ticket_base;
   __syncthreads();
-  const uint64_t tile = s_tile;
-  if (tile >= gridDim.x) {  // ticket out of step with this launch: touch nothing
+  const uint64_t gt = s_tile;
+  if (gt >= gridDim.x) {  // ticket out of step with this launch: touch nothing
     if (tid == 0) atomicCAS(ss.err, kDevOk, kDevTicket);
     return;
+  }
+  // The producer stays an unmodified kernel parameter; product k's residues
+  // are addressed through an explicit word offset.
+  const Producer &prod = prod0;
+  uint64_t tile = gt, first = 0, off = 0;
+  if (batch) {
+    const uint64_t k = gt / tpp;
+    tile = gt - k * tpp;
+    first = k * tpp;
+    off = k * ws_stride;
+    out = batch[k].out;
+    nproc = batch[k].nout < n ? batch[k].nout : n;
   }
   const uint64_t i0 = tile * kCarryTile + static_cast<uint64_t>(tid) * kCarryPer;
 
   V3 v[kCarryPer];
-  prod.eight(i0, nproc, v);
+  prod.eight(off, i0, nproc, v);
   s_prev[tid][0] = v[5].w0; s_prev[tid][1] = v[5].w1; s_prev[tid][2] = v[5].w2;
   s_prev[tid][3] = v[6].w0; s_prev[tid][4] = v[6].w1; s_prev[tid][5] = v[6].w2;
   s_prev[tid][6] = v[7].w0; s_prev[tid][7] = v[7].w1; s_prev[tid][8] = v[7].w2;
   V3 pm3{0, 0, 0}, pm2{0, 0, 0}, pm1{0, 0, 0};
   if (tid == 0 && i0 >= 3) {
-    pm3 = prod(i0 - 3);
-    pm2 = prod(i0 - 2);
-    pm1 = prod(i0 - 1);
+    pm3 = prod.at(off, i0 - 3);
+    pm2 = prod.at(off, i0 - 2);
+    pm1 = prod.at(off, i0 - 1);
   }
   __syncthreads();
   if (tid > 0) {
@@ -276,11 +298,11 @@ __global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer pro
   if (wid == 0) {
     GP agg{0, 1};
     for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
-    const uint32_t cin = look_back_warp(ss, tile, agg, lane);
+    const uint32_t cin = look_back_warp(ss, gt, first, agg, lane);
     if (lane == 0) {
       const uint32_t cout = agg.g | (agg.p & cin);
       __threadfence();
-      reinterpret_cast<volatile unsigned long long *>(ss.flags)[tile] = flag_word(ss.epoch, 2, cout, 0);
+      reinterpret_cast<volatile unsigned long long *>(ss.flags)[gt] = flag_word(ss.epoch, 2, cout, 0);
       s_cin = cin;
       const uint64_t last = tile * kCarryTile + kCarryTile;
       if (last >= nproc && tile * kCarryTile < nproc && cout) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
@@ -288,13 +310,30 @@ __global__ void __launch_bounds__(kCarryThreads) carry_kernel(const Producer pro
   }
   __syncthreads();
   uint32_t cin = excl.g | (excl.p & s_cin);
+  // Stage the tile's limbs in shared memory (reusing s_prev) and store them
+  // with consecutive lanes on consecutive limbs: full 256-byte segments,
+  // which also suits an output that lives in host memory.
+  uint64_t *s_out = &s_prev[0][0];
+  auto oswz = [](uint32_t w) { return w ^ ((w >> 3) & 7u); };
 #pragma unroll
   for (int k = 0; k < kCarryPer; ++k) {
-    const uint64_t i = i0 + k;
     const uint64_t z = al[k] + cin;
     cin = ((gbits >> k) & 1u) | (((pbits >> k) & 1u) & cin);
-    if (i < nproc) out[i] = z;
+    s_out[oswz(static_cast<uint32_t>(tid * kCarryPer + k))] = z;
   }
+  __syncthreads();
+  const uint64_t tbase = tile * kCarryTile;
+#pragma unroll
+  for (int k = 0; k < kCarryPer; ++k) {
+    const uint32_t w = static_cast<uint32_t>(tid + k * kCarryThreads);
+    if (tbase + w < nproc) out[tbase + w] = s_out[oswz(w)];
+  }
+}
+
+// out[N, nout) = 0 for product blockIdx.x.
+__global__ void zero_tails_kernel(const ProductDesc *batch, uint64_t N) {
+  const ProductDesc d = batch[blockIdx.x];
+  for (uint64_t i = N + threadIdx.x; i < d.nout; i += blockDim.x) d.out[i] = 0;
 }
 
 }  // namespace
@@ -309,7 +348,28 @@ cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, 
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   CrtProducer prod{res, n, cc};
-  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                   0, 0, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int logN, const CrtConst &cc,
+                                   const ProductDesc *batch, uint64_t nprod, const ScanState &ss, cudaStream_t st) {
+  const uint64_t n = 1ull << logN;
+  const uint64_t tpp = carry_tiles(n);
+  const uint64_t tiles = tpp * nprod;
+  if (tiles == 0) return cudaSuccess;
+  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  CrtProducer prod{res, n, cc};
+  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, nullptr, 0, ss, batch, tpp,
+                                                                                   ws_stride, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zero_tails(const ProductDesc *batch, uint64_t nprod, uint64_t N, cudaStream_t st) {
+  if (nprod == 0) return cudaSuccess;
+  if (nprod > 0x7fffffffull) return cudaErrorInvalidValue;
+  zero_tails_kernel<<<static_cast<unsigned>(nprod), 256, 0, st>>>(batch, N);
   return cudaGetLastError();
 }
 
@@ -320,7 +380,8 @@ cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   ConvProducer prod{x, nx, y, ny, 0};
-  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                    0, 0, 0);
   return cudaGetLastError();
 }
 
@@ -331,7 +392,8 @@ cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint6
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   ConvProducer prod{x, nx, nullptr, 1, d};
-  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss);
+  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                    0, 0, 0);
   return cudaGetLastError();
 }
 

@@ -9,36 +9,63 @@
 
 namespace hg {
 
-// Device twiddle tables of one prime, all in Montgomery form.
+// Device twiddle tables of one prime.
 struct NttTables {
   const ulonglong2 *sub_fwd;  // (w_4096^e, Shoup companion), e < 2048: sub-transform twiddles, any R <= 4096
   const ulonglong2 *sub_inv;  // (w_4096^-e, companion)
-  const uint64_t *hi_fwd;   // w_{2^30}^(e * 2^15), e < 2^15
-  const uint64_t *lo_fwd;   // w_{2^30}^e,          e < 2^15
+  const uint64_t *hi_fwd;     // w_{2^30}^(e * 2^15), e < 2^15, Montgomery form
+  const uint64_t *lo_fwd;     // w_{2^30}^e,          e < 2^15, Montgomery form
   const uint64_t *hi_inv;
   const uint64_t *lo_inv;
 };
 
-// One NTT pass over a batch of (operand, prime) arrays.  The N residues of
-// an array form blocks of M = R*S; the pass performs the reference's
-// radix-2 stages subn = M .. 2S, i.e. an R-point transform down each of the
-// S columns of every block, followed (forward) or preceded (inverse) by the
-// twiddle w_M^(s * bitrev(r)).
+// One product of a batch, as the kernels read it.  y == nullptr squares x.
+struct ProductDesc {
+  const uint64_t *x, *y;
+  uint64_t nx, ny;
+  uint64_t *out;
+  uint64_t nout;
+};
+
+// One NTT pass over the residue arrays of nprod products x nops operands x
+// nprimes primes.  The N residues of an array form blocks of M = R*S; the
+// pass performs the reference's radix-2 stages subn = M .. 2S, i.e. an
+// R-point transform down each of the S columns of every block, followed
+// (forward) or preceded (inverse) by the twiddle w_M^(s * bitrev(r)).
+// Product k's arrays start at data[op] + k * ws_stride; prime i's at a
+// further (i - prime_lo) * prime_stride.
 struct PassArgs {
-  uint64_t *data[2];         // residues per operand, [kPrimes][N]
-  const uint64_t *limbs[2];  // first forward pass: read limbs and reduce
+  uint64_t *data[2];           // residues per operand
+  const uint64_t *limbs[2];    // single product: this pass reads and reduces limbs
   uint64_t nlimbs[2];
-  int nops;                  // operands handled by this launch
+  const ProductDesc *batch;    // batch: operands of product k are batch[k].x / .y
+  int read_limbs;              // batch: this pass reads and reduces limbs
+  int nops;                    // operands handled by this launch
   int logN;
-  int logR;                  // log2 rows (transform points) of this pass
-  int logS;                  // log2 stride; 0 = contiguous pass
-  int logT;                  // log2 residues per tile
+  int logR;                    // log2 rows (transform points) of this pass
+  int logS;                    // log2 stride; 0 = contiguous pass
+  int logT;                    // log2 residues per tile
   int prime_lo, nprimes;
-  uint64_t prime_stride;     // words between the arrays of consecutive primes
-  uint64_t tiles;            // tiles per (operand, prime)
+  uint64_t prime_stride;       // words between the arrays of consecutive primes
+  uint64_t nprod;              // products in the launch
+  uint64_t ws_stride;          // words between consecutive products' arrays
+  uint64_t tiles;              // tiles per (product, operand, prime)
   PrimeConst pc[kPrimes];
   NttTables tb[kPrimes];
 };
+
+// Limbs a pass reads for (product, operand), or nullptr when it reads residues.
+__host__ __device__ __forceinline__ const uint64_t *pass_limbs(const PassArgs &P, uint64_t prod, int op,
+                                                               uint64_t &nl) {
+  if (P.batch) {
+    if (!P.read_limbs) return nullptr;
+    const ProductDesc &d = P.batch[prod];
+    nl = op ? d.ny : d.nx;
+    return op ? d.y : d.x;
+  }
+  nl = P.nlimbs[op];
+  return P.limbs[op];
+}
 
 // Constants of the Garner reconstruction for one transform length.
 // Each constant is a (value, Shoup companion) pair.
@@ -59,7 +86,7 @@ struct ScanState {
   int *err;                    // device error word
 };
 
-// Kernel launchers (hg_ntt.cu, hg_crt.cu).
+// Kernel launchers.
 // Strided pass (hg_ntt_strided.cu): 4 <= logR <= 8, logT = 12.
 cudaError_t launch_ntt_strided(const PassArgs &a, bool inverse, cudaStream_t st);
 // Contiguous pass (hg_ntt_contig.cu), mode: 0 forward, 1 inverse, 2 product
@@ -68,6 +95,12 @@ constexpr int kContigFwd = 0, kContigInv = 1, kContigMul = 2, kContigSqr = 3;
 cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st);
 cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, uint64_t *out, uint64_t nout,
                              const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
+// Reconstruction + carry for nprod products of transform length 2^logN whose
+// residues start ws_stride words apart at res.
+cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int logN, const CrtConst &cc,
+                                   const ProductDesc *batch, uint64_t nprod, const ScanState &ss, cudaStream_t st);
+// Zero out[N, nout) of every product (out[0, nout) when N == 0).
+cudaError_t launch_zero_tails(const ProductDesc *batch, uint64_t nprod, uint64_t N, cudaStream_t st);
 cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,
                                    uint64_t nout, const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
 cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,

@@ -116,6 +116,11 @@ __device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *da
   }
 }
 
+__device__ __forceinline__ void zero16(uint64_t (&v)[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = 0;
+}
+
 template <int A>
 __device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *data, uint64_t base, uint32_t xt) {
 #pragma unroll
@@ -127,42 +132,53 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
   using Gr = Groups<T>;
   constexpr int ATOP = Gr::template A<Gr::G - 1>();
   constexpr int A0 = Gr::template A<0>();
-  constexpr int NTHR = 1 << (T - 4);
-  constexpr uint32_t HALF = 1u << (T - 1);
+  constexpr int LT = T - 4;                  // log2 threads per block
+  constexpr int BPC = 1 << (kTileBits - T);  // blocks per CTA: every CTA has 256 threads
   extern __shared__ uint64_t smem[];
   const uint32_t tid = threadIdx.x;
-  const int prime = P.prime_lo + static_cast<int>(blockIdx.x % P.nprimes);
-  const uint64_t tile = blockIdx.x / P.nprimes;
+  const uint32_t lt = tid & ((1u << LT) - 1u);  // thread within its block
+  const uint32_t lb = tid >> LT;                // block within the CTA
+  const int prime = P.prime_lo + static_cast<int>(blockIdx.y);
+  const uint64_t nblk = P.nprod * P.tiles;      // blocks of this prime
+  const uint64_t gb = static_cast<uint64_t>(blockIdx.x) * BPC + lb;
+  const bool valid = gb < nblk;                 // idle block slots still take part in barriers
+  const uint64_t prod = valid ? gb / P.tiles : 0;
+  const uint64_t tile = valid ? gb % P.tiles : 0;
   const uint64_t p = P.pc[prime].p;
   const uint32_t c = P.pc[prime].c;
   const NttTables tb = P.tb[prime];
-  const uint64_t poff = static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
+  const uint64_t poff = prod * P.ws_stride + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
   const uint64_t base = tile << T;
 
   constexpr bool TWO = (MODE == kMul);
-  uint64_t *smA = smem;
-  uint64_t *smB = smem + (TWO ? (1u << T) : 0u);
+  uint64_t *smA = smem + (lb << T);
+  uint64_t *smB = smem + ((BPC + lb) << T);
   // One table of (twiddle, companion) pairs: the forward one, replaced by
   // the inverse one after the pointwise product.
-  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) << T));
-  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, NTHR);
+  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) << kTileBits));
+  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, kTileThreads);
+  uint64_t nl0 = 0, nl1 = 0;
+  const uint64_t *limbs0 = pass_limbs(P, prod, 0, nl0);
+  const uint64_t *limbs1 = TWO ? pass_limbs(P, prod, 1, nl1) : nullptr;
 
   uint64_t v[16];
   uint32_t xt;
   if constexpr (MODE == kInv) {
-    xt = thread_base<A0>(tid);
-    load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
+    xt = thread_base<A0>(lt);
+    if (valid) load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
+    else zero16(v);
     __syncthreads();
-    inverse_rounds<T>(v, smA, tw, xt, tid, p, c);
-    store_block<ATOP>(v, P.data[0] + poff, base, xt);
+    inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
+    if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
   } else {
-    xt = thread_base<ATOP>(tid);
-    load_block<ATOP>(v, P.data[0] + poff, P.limbs[0], P.nlimbs[0], base, xt, p);
+    xt = thread_base<ATOP>(lt);
+    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
+    else zero16(v);
     __syncthreads();
-    forward_rounds<T>(v, smA, tw, xt, tid, p, c);
+    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
     if constexpr (MODE == kFwd) {
-      store_block<A0>(v, P.data[0] + poff, base, xt);
+      if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
       return;
     } else {
       if constexpr (MODE == kMul) {
@@ -170,9 +186,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
         // words), transform operand 1 through smB.
         __syncthreads();
         to_smem<A0>(smA, v, xt);
-        uint32_t xb = thread_base<ATOP>(tid);
-        load_block<ATOP>(v, P.data[1] + poff, P.limbs[1], P.nlimbs[1], base, xb, p);
-        forward_rounds<T>(v, smB, tw, xb, tid, p, c);
+        uint32_t xb = thread_base<ATOP>(lt);
+        if (valid) load_block<ATOP>(v, P.data[1] + poff, limbs1, nl1, base, xb, p);
+        else zero16(v);
+        forward_rounds<T>(v, smB, tw, xb, lt, p, c);
         const uint32_t sx = swz(xb);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(smA[sx ^ swz(static_cast<uint32_t>(i) << A0)], v[i], p, c);
@@ -183,29 +200,33 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
       __syncthreads();  // every thread is done with the forward table
-      load_sub_twiddles(tw, tb.sub_inv, T, tid, NTHR);
+      load_sub_twiddles(tw, tb.sub_inv, T, tid, kTileThreads);
       __syncthreads();
-      inverse_rounds<T>(v, smA, tw, xt, tid, p, c);
-      store_block<ATOP>(v, P.data[0] + poff, base, xt);
+      inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
+      if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     }
   }
 }
 
-// Transforms of 2, 4 or 8 points: the reference's loops, one thread per prime.
+// Transforms of 2, 4 or 8 points: the reference's loops, one thread per
+// (product, prime).
 __global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
-  const int prime = P.prime_lo + static_cast<int>(blockIdx.x % P.nprimes);
+  const uint64_t prod = blockIdx.x;
+  const int prime = P.prime_lo + static_cast<int>(blockIdx.y);
   const uint64_t p = P.pc[prime].p;
   const uint32_t c = P.pc[prime].c;
   const NttTables tb = P.tb[prime];
-  const uint64_t poff = static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
+  const uint64_t poff = prod * P.ws_stride + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
   const int L = P.logN;
   const int n = 1 << L;
   uint64_t a[2][8];
   const int nops = mode == kMul ? 2 : 1;
-  for (int op = 0; op < nops; ++op)
+  for (int op = 0; op < nops; ++op) {
+    uint64_t nl = 0;
+    const uint64_t *limbs = pass_limbs(P, prod, op, nl);
     for (int i = 0; i < n; ++i)
-      a[op][i] = P.limbs[op] ? (static_cast<uint64_t>(i) < P.nlimbs[op] ? reduce64(P.limbs[op][i], p) : 0)
-                             : P.data[op][poff + i];
+      a[op][i] = limbs ? (static_cast<uint64_t>(i) < nl ? reduce64(limbs[i], p) : 0) : P.data[op][poff + i];
+  }
   if (mode != kInv) {
     for (int op = 0; op < nops; ++op)
       for (int ls = L; ls >= 1; --ls) {  // DIF, subn = 2^ls
@@ -245,19 +266,28 @@ __global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, ui
 }
 
 template <int T, int MODE>
-cudaError_t launch_tm(const PassArgs &a, unsigned grid, cudaStream_t st) {
-  constexpr size_t bytes = ((MODE == kMul ? 2u : 1u) << T) * sizeof(uint64_t) + (1u << (T - 1)) * sizeof(ulonglong2);
-  if (bytes > 48 * 1024) {
+cudaError_t launch_tm(const PassArgs &a, dim3 grid, cudaStream_t st) {
+  constexpr size_t bytes =
+      ((MODE == kMul ? 2u : 1u) << kTileBits) * sizeof(uint64_t) + (1u << (T - 1)) * sizeof(ulonglong2);
+  // Raise the dynamic shared-memory limit once per instantiation (not on
+  // every launch, so that launches can be captured in a CUDA graph).
+  static bool raised = false;
+  if (bytes > 48 * 1024 && !raised) {
     cudaError_t e = cudaFuncSetAttribute(ntt_contig_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(bytes));
     if (e != cudaSuccess) return e;
+    raised = true;
   }
-  ntt_contig_kernel<T, MODE><<<grid, 1 << (T - 4), bytes, st>>>(a);
+  ntt_contig_kernel<T, MODE><<<grid, kTileThreads, bytes, st>>>(a);
   return cudaGetLastError();
 }
 
 template <int MODE>
-cudaError_t launch_mode(const PassArgs &a, unsigned grid, cudaStream_t st) {
+cudaError_t launch_mode(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
+  const uint64_t bpc = 1ull << (kTileBits - a.logT);
+  const uint64_t gx = (nblk + bpc - 1) / bpc;
+  if (gx == 0 || gx > 0x7fffffffull) return cudaErrorInvalidValue;
+  const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(a.nprimes));
   switch (a.logT) {
     case 4: return launch_tm<4, MODE>(a, grid, st);
     case 5: return launch_tm<5, MODE>(a, grid, st);
@@ -275,19 +305,19 @@ cudaError_t launch_mode(const PassArgs &a, unsigned grid, cudaStream_t st) {
 }  // namespace
 
 cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
-  const uint64_t grid = a.tiles * static_cast<uint64_t>(a.nprimes);
-  if (grid == 0 || grid > 0x7fffffffull || a.logS != 0 || a.logR != a.logT) return cudaErrorInvalidValue;
-  const unsigned g = static_cast<unsigned>(grid);
+  const uint64_t nblk = a.tiles * a.nprod;  // blocks per prime
+  if (nblk == 0 || a.logS != 0 || a.logR != a.logT || a.nprimes < 1 || a.nprimes > kPrimes)
+    return cudaErrorInvalidValue;
   if (a.logT < 4) {
-    if (a.logT < 1 || a.logT != a.logN) return cudaErrorInvalidValue;
-    ntt_tiny_kernel<<<g, 1, 0, st>>>(a, mode);
+    if (a.logT < 1 || a.logT != a.logN || a.tiles != 1 || a.nprod > 0x7fffffffull) return cudaErrorInvalidValue;
+    ntt_tiny_kernel<<<dim3(static_cast<unsigned>(a.nprod), static_cast<unsigned>(a.nprimes)), 1, 0, st>>>(a, mode);
     return cudaGetLastError();
   }
   switch (mode) {
-    case kFwd: return launch_mode<kFwd>(a, g, st);
-    case kInv: return launch_mode<kInv>(a, g, st);
-    case kMul: return launch_mode<kMul>(a, g, st);
-    case kSqr: return launch_mode<kSqr>(a, g, st);
+    case kFwd: return launch_mode<kFwd>(a, nblk, st);
+    case kInv: return launch_mode<kInv>(a, nblk, st);
+    case kMul: return launch_mode<kMul>(a, nblk, st);
+    case kSqr: return launch_mode<kSqr>(a, nblk, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -42,12 +42,14 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
   const int prime = P.prime_lo + static_cast<int>(bid % P.nprimes);
   bid /= P.nprimes;
   const int op = static_cast<int>(bid % P.nops);
-  const uint64_t tile = bid / P.nops;
+  bid /= P.nops;
+  const uint64_t prod = bid / P.tiles;
+  const uint64_t tile = bid % P.tiles;
 
   const uint64_t p = P.pc[prime].p;
   const uint32_t c = P.pc[prime].c;
   const NttTables tb = P.tb[prime];
-  uint64_t *data = P.data[op] + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
+  uint64_t *data = P.data[op] + prod * P.ws_stride + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
   const int logS = P.logS;
   const int logM = LOGR + logS;
   const uint64_t ncg = 1ull << (logS - LOGTC);
@@ -78,9 +80,9 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
     uint32_t xt = thread_base<AL>(tid);
     uint64_t off, step;
     offsets(xt, AL, off, step);
-    const uint64_t *limbs = P.limbs[op];
+    uint64_t nl = 0;
+    const uint64_t *limbs = pass_limbs(P, prod, op, nl);
     if (limbs) {
-      const uint64_t nl = P.nlimbs[op];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const uint64_t o = off + i * step;
@@ -141,7 +143,7 @@ cudaError_t launch_r(const PassArgs &a, bool inverse, unsigned grid, cudaStream_
 }  // namespace
 
 cudaError_t launch_ntt_strided(const PassArgs &a, bool inverse, cudaStream_t st) {
-  const uint64_t grid = a.tiles * static_cast<uint64_t>(a.nops) * static_cast<uint64_t>(a.nprimes);
+  const uint64_t grid = a.tiles * a.nprod * static_cast<uint64_t>(a.nops) * static_cast<uint64_t>(a.nprimes);
   if (grid == 0 || grid > 0x7fffffffull || a.logT != kTileBits || a.logS < kTileBits - a.logR)
     return cudaErrorInvalidValue;
   const unsigned g = static_cast<unsigned>(grid);

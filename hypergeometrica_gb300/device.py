@@ -53,3 +53,50 @@ def ntt_reverse(a, mod_num: int, stream=None) -> None:
 def sync(stream=None) -> None:
     """Wait and surface device-side errors (hg_sync)."""
     check(load().hg_sync(None if stream is None else _stream(stream)))
+
+
+def _products(items):
+    """hg_product array from (x, y_or_None, out[, nx, ny]) tensor tuples."""
+    from ._lib import HgProduct
+
+    arr = (HgProduct * len(items))()
+    for k, it in enumerate(items):
+        x, y, out = it[0], it[1], it[2]
+        nx = it[3] if len(it) > 3 and it[3] is not None else x.numel()
+        ny = (it[4] if len(it) > 4 and it[4] is not None else y.numel()) if y is not None else 0
+        arr[k] = HgProduct(_p(x), nx, None if y is None else _p(y), ny, _p(out), out.numel())
+    return arr
+
+
+class Batch:
+    """A planned batch of products (hg_batch_create); run() enqueues it on a
+    stream and can be captured in a CUDA graph.  Keeps the tensors alive."""
+
+    def __init__(self, items, autotune: bool = True):
+        import ctypes
+
+        from ._lib import HG_BATCH_AUTOTUNE
+
+        self._items = list(items)
+        self._arr = _products(self._items)
+        h = ctypes.c_void_p()
+        check(load().hg_batch_create(self._arr, len(self._items), HG_BATCH_AUTOTUNE if autotune else 0,
+                                     ctypes.byref(h)))
+        self._h = h
+
+    def run(self, stream=None) -> None:
+        check(load().hg_batch_run(self._h, _stream(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().hg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def mul_batch(items, stream=None) -> None:
+    """One-shot batch (hg_mul_batch_device): items are (x, y_or_None, out)."""
+    arr = _products(items)
+    check(load().hg_mul_batch_device(arr, len(items), _stream(stream)))

@@ -111,6 +111,40 @@ int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, siz
  * error latched on the device since the last hg_sync. */
 int hg_sync(void *stream);
 
+/* ---- batches of products on device memory ----------------------------
+ * No counterpart in the reference, which multiplies one pair at a time.  Its
+ * binary splitting issues thousands of independent products per tree level
+ * (combine, src/binary-splitting.lisp:112-121); a batch runs them together:
+ * products are grouped by transform length and each group runs as one
+ * launch per NTT pass, with the pass split per length chosen by timing the
+ * candidates (HG_BATCH_AUTOTUNE).  hg_batch_run enqueues kernels and
+ * memsets only, so it can be captured in a CUDA graph and replayed; a batch
+ * owns its workspace, so batches on different streams may overlap. */
+typedef struct hg_product {
+    const uint64_t *x; /* device limbs                                   */
+    size_t nx;
+    const uint64_t *y; /* device limbs; NULL squares x (mpz-square)      */
+    size_t ny;
+    uint64_t *out;     /* device result, nout >= nx + ny limbs (2nx square) */
+    size_t nout;
+} hg_product;
+
+typedef struct hg_batch hg_batch;
+#define HG_BATCH_AUTOTUNE 1 /* time the candidate pass splits for each length */
+
+/* Plan a batch (sizes as given: device operands are not trimmed), allocate
+ * its workspace and, with HG_BATCH_AUTOTUNE, run each group once per
+ * candidate schedule to pick the fastest.  Must not be called while a
+ * stream is being captured. */
+int hg_batch_create(const hg_product *prods, size_t n, int flags, hg_batch **batch);
+/* Enqueue every product of the batch on stream. */
+int hg_batch_run(hg_batch *batch, void *stream);
+/* Free a batch (after its work has completed). */
+int hg_batch_destroy(hg_batch *batch);
+/* One-shot: create (no tuning, schedules from earlier tuning are reused),
+ * run on stream, wait, destroy. */
+int hg_mul_batch_device(const hg_product *prods, size_t n, void *stream);
+
 /* ---- spectra (parity hooks) -------------------------------------------- */
 
 /* ntt-forward (src/number-theoretic-transform.lisp:40-90) in place on n
