@@ -73,6 +73,7 @@ SIGNATURES = {
     "hg_mul_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
     "hg_sqr_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp]),
     "hg_mul_schoolboy_device": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
+    "hg_mul_device_noalloc": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz, _vp]),
     "hg_sync": (ctypes.c_int, [_vp]),
     "hg_batch_create": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, ctypes.c_int, ctypes.POINTER(_vp)]),
     "hg_batch_run": (ctypes.c_int, [_vp, _vp]),

@@ -499,6 +499,108 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   return HG_OK;
 }
 
+// ---- products on a fixed scratch array (hg_mul_device_noalloc) ----------
+//
+// Scratch layout, in words: operand 0's residues [3][2^16], operand 1's
+// residues [3][2^16], the carry scan's ticket word, then one flag word per
+// carry tile (32 at 2^16).  Static device memory is zero when the module
+// loads; the residue area needs no initial value (the first pass writes
+// every word it later reads), and the call clears the ticket and flag words
+// on its stream before each reconstruction.
+constexpr int kNoAllocLogN = 16;
+constexpr uint64_t kNoAllocN = uint64_t(1) << kNoAllocLogN;
+constexpr uint64_t kNoAllocResWords = 2ull * kPrimes * kNoAllocN;
+constexpr uint64_t kNoAllocScanWords = 64;
+constexpr int kNoAllocDevices = 64;
+static_assert(kNoAllocN == HG_NOALLOC_MAX_LIMBS, "public limit and scratch size disagree");
+
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocResWords + kNoAllocScanWords];
+
+// Device address of g_noalloc_scratch per device ordinal, looked up once.
+uint64_t *g_noalloc_ptr[kNoAllocDevices] = {};
+
+// ntt_product_device's schedule on the static scratch: at 2^L <= 2^16 the
+// plan is one contiguous pass (L <= 12) or one 4-bit strided pass around an
+// (L - 4)-bit contiguous block, launched here without the growing workspace,
+// the shared scan state or the profiling events of the general path.
+int noalloc_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,
+                           uint64_t nout, cudaStream_t st) {
+  Context &c = g_ctx;
+  const bool square = (y == nullptr);
+  if (square) ny = nx;
+  const uint64_t size = nx + ny;
+  if (!out || (nx && !x) || (!square && ny && !y)) return fail(HG_ERR_ARG, "null pointer");
+  if (nout < size) return fail(HG_ERR_ARG, "nout = %llu cannot hold the %llu-limb product", (unsigned long long)nout,
+                               (unsigned long long)size);
+  if (size > kNoAllocN)
+    return fail(HG_ERR_ARG, "hg_mul_device_noalloc: a %llu-limb product exceeds its fixed scratch limit of %llu limbs",
+                (unsigned long long)size, (unsigned long long)kNoAllocN);
+  int dev = -1;
+  HG_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev != c.device)
+    return fail(HG_ERR_ARG, "hg_mul_device_noalloc: current device %d is not the library's device %d", dev, c.device);
+  if (dev < 0 || dev >= kNoAllocDevices) return fail(HG_ERR_ARG, "device ordinal %d out of range", dev);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    HG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch), "scratch address lookup");
+    g_noalloc_ptr[dev] = static_cast<uint64_t *>(p);
+  }
+  uint64_t *scratch = g_noalloc_ptr[dev];
+  if (nx == 0 || ny == 0) {
+    HG_CUDA(cudaMemsetAsync(out, 0, nout * sizeof(uint64_t), st), "zero product");
+    return HG_OK;
+  }
+  const int L = ilog2_ceil(size);
+  const uint64_t N = uint64_t(1) << L;
+  const int logC = L <= kTileBits ? L : L - 4;  // contiguous block bits
+  PassArgs a = base_args(L, square ? 1 : 2);
+  a.data[0] = scratch;
+  a.data[1] = scratch + kPrimes * kNoAllocN;
+  a.limbs[0] = x;
+  a.limbs[1] = square ? nullptr : y;
+  a.nlimbs[0] = nx;
+  a.nlimbs[1] = square ? 0 : ny;
+  if (L > kTileBits) {
+    PassArgs f = a;
+    f.logR = 4;
+    f.logS = logC;
+    f.logT = kTileBits;
+    f.tiles = N >> kTileBits;
+    HG_CUDA(launch_ntt_strided(f, false, st), "forward transform");
+    a.limbs[0] = a.limbs[1] = nullptr;
+  }
+  a.logR = logC;
+  a.logS = 0;
+  a.logT = logC;
+  a.tiles = N >> logC;
+  HG_CUDA(launch_ntt_contig(a, square ? kContigSqr : kContigMul, st), "middle pass");
+  if (L > kTileBits) {
+    PassArgs inv = base_args(L, 1);
+    inv.data[0] = scratch;
+    inv.logR = 4;
+    inv.logS = logC;
+    inv.logT = kTileBits;
+    inv.tiles = N >> kTileBits;
+    HG_CUDA(launch_ntt_strided(inv, true, st), "inverse transform");
+  }
+  if (nout > N) HG_CUDA(cudaMemsetAsync(out + N, 0, (nout - N) * sizeof(uint64_t), st), "zero tail");
+  const uint64_t nproc = nout < N ? nout : N;
+  const uint64_t tiles = carry_tiles(nproc);
+  if (tiles + 1 > kNoAllocScanWords) return fail(HG_ERR_ARG, "carry scan of %llu tiles exceeds the scratch",
+                                                 (unsigned long long)tiles);
+  uint64_t *scan = scratch + kNoAllocResWords;
+  HG_CUDA(cudaMemsetAsync(scan, 0, (tiles + 1) * sizeof(uint64_t), st), "scan state reset");
+  ScanState ss;
+  ss.ticket = reinterpret_cast<unsigned long long *>(scan);
+  ss.ticket_base = 0;
+  ss.flags = reinterpret_cast<unsigned long long *>(scan + 1);
+  ss.epoch = 1;
+  ss.err = reinterpret_cast<int *>(static_cast<char *>(c.misc.p) + 8);
+  uint64_t used = 0;
+  HG_CUDA(launch_crt_carry(scratch, L, crt_const(L), out, nout, ss, st, &used), "reconstruction");
+  return HG_OK;
+}
+
 int small_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t d, uint64_t *out,
                          uint64_t nout, cudaStream_t st) {
   const uint64_t size = y ? nx + ny : nx + 1;
@@ -1064,6 +1166,13 @@ int hg_sqr_device(const uint64_t *x, size_t nx, uint64_t *out, size_t nout, void
   int rc = ensure_init();
   if (rc) return rc;
   return ntt_product_device(x, nx, nullptr, 0, out, nout, static_cast<cudaStream_t>(stream));
+}
+
+int hg_mul_device_noalloc(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
+                          void *stream) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  if (!g_ctx.ready) return fail(HG_ERR_NOT_INIT, "hg_mul_device_noalloc: call hg_init first");
+  return noalloc_product_device(x, nx, y, ny, out, nout, static_cast<cudaStream_t>(stream));
 }
 
 int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,

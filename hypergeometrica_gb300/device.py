@@ -36,6 +36,19 @@ def sqr(x, out, nx=None, stream=None) -> None:
     check(load().hg_sqr_device(_p(x), nx, _p(out), out.numel(), _stream(stream)))
 
 
+NOALLOC_MAX_LIMBS = 65536
+
+
+def mul_noalloc(x, y, out, nx=None, ny=None, stream=None) -> None:
+    """|x| * |y| (|x|^2 when y is None) into out on the library's fixed
+    scratch (hg_mul_device_noalloc): no allocation, at most
+    NOALLOC_MAX_LIMBS product limbs, calls on one stream at a time."""
+    nx = x.numel() if nx is None else nx
+    ny = (nx if y is None else y.numel()) if ny is None else ny
+    yp = None if y is None else _p(y)
+    check(load().hg_mul_device_noalloc(_p(x), nx, yp, ny, _p(out), out.numel(), _stream(stream)))
+
+
 def mul_schoolboy(x, y, out, stream=None) -> None:
     check(load().hg_mul_schoolboy_device(_p(x), x.numel(), _p(y), y.numel(), _p(out), out.numel(), _stream(stream)))
 

@@ -107,6 +107,41 @@ int hg_sqr_device(const uint64_t *x, size_t nx, uint64_t *out, size_t nout, void
 int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out,
                             size_t nout, void *stream);
 
+/* ---- products without allocation -------------------------------------- */
+
+/* Largest product (nx + ny limbs, transform length 2^16) that
+ * hg_mul_device_noalloc accepts. */
+#define HG_NOALLOC_MAX_LIMBS 65536
+
+/* No counterpart in the reference: hypergeometrica allocates its transform
+ * storage per product.  Same result as hg_mul_device (hg_sqr_device when y
+ * is NULL) for products of at most HG_NOALLOC_MAX_LIMBS limbs, computed in a
+ * 3 MiB scratch array compiled into the library, so the call makes no
+ * device or pinned allocation.  It is for callers that must not allocate
+ * while they run: a cudaMalloc or cudaFree synchronises the whole device,
+ * and a process that has handed its device memory to its own pool or arena
+ * may have none left for the library's grow-only workspace.
+ *
+ *  - hg_init must have succeeded first (HG_ERR_NOT_INIT otherwise); the call
+ *    never initialises the library itself, because that allocates.
+ *  - The first call on a device does a one-time setup: with the library's
+ *    device current it looks up the scratch array's device address
+ *    (cudaGetSymbolAddress).  Make that first call before any stream
+ *    capture begins.  A call with another device current is HG_ERR_ARG.
+ *  - nx + ny > HG_NOALLOC_MAX_LIMBS is rejected with HG_ERR_ARG before
+ *    anything is enqueued.
+ *  - The carry scan's ticket and flag words in the scratch must be zero
+ *    when its kernel starts; the call clears them on stream itself
+ *    (cudaMemsetAsync), so the caller zeroes nothing.
+ *  - There is one scratch array per device, shared by every call: calls
+ *    whose work can overlap on the GPU (different streams without an event
+ *    between them, or several host threads) race and corrupt each other's
+ *    results.  Issue them on one stream, or order them with events.
+ *    hg_mul_device and the batch API use other storage and do not race
+ *    with it. */
+int hg_mul_device_noalloc(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
+                          void *stream);
+
 /* Wait for the library's work on stream (NULL = all of it) and report any
  * error latched on the device since the last hg_sync. */
 int hg_sync(void *stream);
