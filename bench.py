@@ -222,6 +222,92 @@ def _residue_ok(out_u64, x_u64, y_u64) -> bool:
     return full(out_u64) == full(x_u64) * full(y_u64) % q
 
 
+BATCH_PAIRS = 4096
+
+
+def run_batched(stream, steps: int) -> dict:
+    """4096 independent pairs, sizes log-uniform in [2^6, 2^14] limbs per
+    operand (seeds 41, 42), uniform limbs: the binary-splitting-leaf workload.
+    Times an autotuned batch replayed from a CUDA graph against one
+    hg_mul_device call per product on the same stream; both must agree on
+    every product."""
+    import numpy as np
+    import torch
+
+    from hypergeometrica_gb300 import _lib
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import workloads as W
+
+    sx = W.log_uniform_sizes(41, BATCH_PAIRS, 6, 14)
+    sy = W.log_uniform_sizes(42, BATCH_PAIRS, 6, 14)
+    host = np.concatenate([W.limbs(100_000 + k, int(sx[k]) + int(sy[k])) for k in range(BATCH_PAIRS)])
+    ops = torch.from_numpy(host.view(np.int64)).cuda()
+    nout = int((sx + sy).sum())
+    out_pp = torch.zeros(nout, dtype=torch.int64, device="cuda")
+    out_b = torch.full((nout,), -1, dtype=torch.int64, device="cuda")
+    pp, items = [], []
+    o = 0
+    for k in range(BATCH_PAIRS):
+        nx, ny = int(sx[k]), int(sy[k])
+        x, y = ops[o: o + nx], ops[o + nx: o + nx + ny]
+        pp.append((x, y, out_pp[o: o + nx + ny]))
+        items.append((x, y, out_b[o: o + nx + ny]))
+        o += nx + ny
+
+    def per_product():
+        for x, y, out in pp:
+            D.mul(x, y, out, stream=stream)
+
+    per_product()
+    D.sync(stream)
+    t0 = time.perf_counter()
+    b = D.Batch(items, autotune=True)
+    tune_s = time.perf_counter() - t0
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        b.run(s)
+    s.synchronize()
+    _lib.profile_read()
+    b.run(stream)
+    D.sync(stream)
+    launches_batch = sum(v["launches"] for v in _lib.profile_read().values())
+    per_product()
+    D.sync(stream)
+    launches_pp = sum(v["launches"] for v in _lib.profile_read().values())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        b.run(s)
+    out_b.fill_(-1)
+    g.replay()
+    torch.cuda.synchronize()
+    D.sync(stream)
+    correct = bool(torch.equal(out_b, out_pp))
+
+    def timed(fn, reps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    with torch.cuda.stream(stream):
+        ms_graph = timed(g.replay, max(3, steps))
+    ms_pp = timed(per_product, max(2, min(steps, 5)))
+    D.sync(stream)
+    return {
+        "metric": "products/s, 4096 uneven pairs", "unit": "products/s",
+        "workload": f"{BATCH_PAIRS} pairs, operand sizes log-uniform in [2^6, 2^14] limbs (seeds 41, 42), "
+                    f"{nout} output limbs",
+        "graph": BATCH_PAIRS / (ms_graph / 1000.0), "per_product": BATCH_PAIRS / (ms_pp / 1000.0),
+        "speedup": ms_pp / ms_graph, "ms_graph": ms_graph, "ms_per_product_path": ms_pp,
+        "gpu_launches_graph": launches_batch, "gpu_launches_per_product_path": launches_pp,
+        "autotune_s": tune_s, "correct": correct,
+    }
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -342,6 +428,9 @@ def run_ours(args) -> None:
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"],
                    "samples": clocks["samples"]},
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(stream, args.steps)
+        line["correct"] = line["correct"] and line["batched"]["correct"]
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cores, model = _cpu_info()
         threads = min(6, cores)
@@ -364,6 +453,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--log-size", type=int, default=LOG_SIZE, help="log2 limbs per operand (default 24)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 4096-pair batched-products measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
