@@ -57,6 +57,17 @@ class HgProduct(ctypes.Structure):
 
 HG_BATCH_AUTOTUNE = 1
 
+
+class HgSvcStats(ctypes.Structure):
+    """hg_svc_report: counters and submit-to-completion latency of a service."""
+
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("pending", ctypes.c_uint64), ("in_flight", ctypes.c_uint64),
+                ("peak_batch_products", ctypes.c_uint64), ("peak_batch_workspace_bytes", ctypes.c_uint64),
+                ("slot_workspace_bytes", ctypes.c_uint64), ("latency_samples", ctypes.c_uint64),
+                ("slots", ctypes.c_int), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
+                ("mean_us", ctypes.c_double), ("max_us", ctypes.c_double), ("products_per_s", ctypes.c_double)]
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "hg_init": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int]),
@@ -79,6 +90,13 @@ SIGNATURES = {
     "hg_batch_run": (ctypes.c_int, [_vp, _vp]),
     "hg_batch_destroy": (ctypes.c_int, [_vp]),
     "hg_mul_batch_device": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, _vp]),
+    "hg_svc_open": (ctypes.c_int, [_sz, ctypes.c_int, _sz, ctypes.POINTER(_vp)]),
+    "hg_svc_submit": (ctypes.c_int, [_vp, ctypes.POINTER(HgProduct), _sz, ctypes.POINTER(ctypes.c_uint64)]),
+    "hg_svc_status": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "hg_svc_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_double]),
+    "hg_svc_wait_all": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "hg_svc_stats": (ctypes.c_int, [_vp, ctypes.POINTER(HgSvcStats), ctypes.c_int]),
+    "hg_svc_close": (ctypes.c_int, [_vp]),
     "hg_ntt_forward_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
     "hg_ntt_reverse_device": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp]),
     "hg_profile_enable": (ctypes.c_int, [ctypes.c_int]),

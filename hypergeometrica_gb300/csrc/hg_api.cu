@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -18,7 +19,7 @@
 #include <tuple>
 #include <vector>
 
-#include "hg_internal.h"
+#include "hg_host.h"
 #include "hypergeometrica_gb300.h"
 
 namespace hg {
@@ -295,10 +296,6 @@ uint64_t trimmed(const uint64_t *x, uint64_t n) {
   while (n > 0 && x[n - 1] == 0) --n;
   return n;
 }
-
-struct PassPlan {
-  int logR, logS, logT;
-};
 
 // Passes for N = 2^L: strided passes of 4..8 row bits over 4096-residue tiles
 // (>= 16 columns, i.e. >= 128-byte row segments), then one contiguous pass
@@ -754,15 +751,6 @@ int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) 
 // ---- batches -------------------------------------------------------------
 
 // Products of one transform length (and kind) run by one launch per pass.
-struct BatchGroup {
-  int L = 0;
-  bool square = false;
-  bool tails = false;              // some product has nout > N
-  std::vector<PassPlan> plan;
-  uint64_t first = 0, nprod = 0;   // descriptors [first, first + nprod)
-  uint64_t flags_off = 0;          // first carry-scan flag word
-};
-
 // Candidate pass splits of a 2^L transform: the default plan and, for
 // L >= 12, every contiguous block size T with the remaining L - T bits in
 // as few strided passes of 4..8 bits as possible.
@@ -801,25 +789,22 @@ std::map<std::tuple<int, bool, uint64_t>, std::vector<PassPlan>> g_tuned;
 }  // namespace hg
 
 struct hg_batch {
-  std::vector<hg::BatchGroup> groups;
-  std::vector<hg::ProductDesc> desc;  // groups contiguous, then the zero products
-  uint64_t zero_first = 0, nzero = 0;
-  uint64_t ws_words = 0, flag_words = 0;
+  hg::BatchPlan bp;
   hg::DevBuf d_desc, ws, flags, tickets;
 };
 
 namespace hg {
 namespace {
 
-// Enqueue one group with the given schedule.  The group's ticket and flags
+// Enqueue group gi with the given schedule.  The group's ticket and flags
 // must be zero.
-int run_group(hg_batch *b, size_t gi, const std::vector<PassPlan> &plan, cudaStream_t st) {
-  const BatchGroup &g = b->groups[gi];
+int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::vector<PassPlan> &plan,
+              cudaStream_t st) {
   const int nops = g.square ? 1 : 2;
   const uint64_t N = uint64_t(1) << g.L;
   const uint64_t slab = static_cast<uint64_t>(kPrimes) * N;
-  const ProductDesc *d = static_cast<const ProductDesc *>(b->d_desc.p) + g.first;
-  uint64_t *ws = b->ws.u64();
+  const ProductDesc *d = bb.desc + g.first;
+  uint64_t *ws = bb.ws;
   if (g.tails) HG_CUDA(launch_zero_tails(d, g.nprod, N, st), "zero tails");
   PassArgs a = base_args(g.L, nops);
   a.batch = d;
@@ -839,11 +824,11 @@ int run_group(hg_batch *b, size_t gi, const std::vector<PassPlan> &plan, cudaStr
   inv.data[0] = ws;
   HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
   ScanState ss;
-  ss.ticket = static_cast<unsigned long long *>(b->tickets.p) + gi;
+  ss.ticket = bb.tickets + gi;
   ss.ticket_base = 0;
-  ss.flags = static_cast<unsigned long long *>(b->flags.p) + g.flags_off;
+  ss.flags = bb.flags + g.flags_off;
   ss.epoch = 1;
-  ss.err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
+  ss.err = bb.err;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(N) * static_cast<double>(g.nprod));
     HG_CUDA(launch_crt_carry_batch(ws, slab, g.L, crt_const(g.L), d, g.nprod, ss, st), "reconstruction");
@@ -851,11 +836,16 @@ int run_group(hg_batch *b, size_t gi, const std::vector<PassPlan> &plan, cudaStr
   return HG_OK;
 }
 
-int batch_clear_scan(hg_batch *b, cudaStream_t st) {
-  if (b->flag_words) HG_CUDA(cudaMemsetAsync(b->flags.p, 0, b->flag_words * 8, st), "scan flags reset");
-  if (!b->groups.empty())
-    HG_CUDA(cudaMemsetAsync(b->tickets.p, 0, b->groups.size() * 8, st), "scan tickets reset");
+int batch_clear_scan(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) {
+  if (bp.flag_words) HG_CUDA(cudaMemsetAsync(bb.flags, 0, bp.flag_words * 8, st), "scan flags reset");
+  if (!bp.groups.empty()) HG_CUDA(cudaMemsetAsync(bb.tickets, 0, bp.groups.size() * 8, st), "scan tickets reset");
   return HG_OK;
+}
+
+BatchBufs batch_bufs(hg_batch *b) {
+  return BatchBufs{static_cast<const ProductDesc *>(b->d_desc.p), b->ws.u64(),
+                   static_cast<unsigned long long *>(b->flags.p), static_cast<unsigned long long *>(b->tickets.p),
+                   reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8)};
 }
 
 // Time each candidate schedule of each group (twice; the second run counts)
@@ -866,8 +856,9 @@ int batch_autotune(hg_batch *b) {
   HG_CUDA(cudaEventCreate(&e0), "event creation");
   HG_CUDA(cudaEventCreate(&e1), "event creation");
   int rc = HG_OK;
-  for (size_t gi = 0; gi < b->groups.size() && rc == HG_OK; ++gi) {
-    BatchGroup &g = b->groups[gi];
+  const BatchBufs bb = batch_bufs(b);
+  for (size_t gi = 0; gi < b->bp.groups.size() && rc == HG_OK; ++gi) {
+    BatchGroup &g = b->bp.groups[gi];
     const auto key = std::make_tuple(g.L, g.square, g.nprod);
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -882,9 +873,9 @@ int batch_autotune(hg_batch *b) {
     for (const auto &plan : cands) {
       float ms = 0;
       for (int rep = 0; rep < 2 && rc == HG_OK; ++rep) {
-        if ((rc = batch_clear_scan(b, st))) break;
+        if ((rc = batch_clear_scan(b->bp, bb, st))) break;
         cudaEventRecord(e0, st);
-        if ((rc = run_group(b, gi, plan, st))) break;
+        if ((rc = run_group(g, gi, bb, plan, st))) break;
         cudaEventRecord(e1, st);
         if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(HG_ERR_CUDA, "autotune timing failed");
         else cudaEventElapsedTime(&ms, e0, e1);
@@ -908,16 +899,11 @@ int batch_autotune(hg_batch *b) {
 
 constexpr uint64_t kBatchWorkspaceCap = uint64_t(4) << 30;  // bytes per group chunk
 
-int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
-  if (!out || (n && !prods)) return fail(HG_ERR_ARG, "null pointer");
-  *out = nullptr;
-  std::unique_ptr<hg_batch> b(new hg_batch());
-  struct Item {
-    int L;
-    bool square;
-    size_t i;
-  };
-  std::vector<Item> items, zeros;
+// Validate the C-ABI product list into descriptors.
+int product_descs(const hg_product *prods, size_t n, std::vector<ProductDesc> &out) {
+  if (n && !prods) return fail(HG_ERR_ARG, "null pointer");
+  out.clear();
+  out.reserve(n);
   for (size_t i = 0; i < n; ++i) {
     const hg_product &p = prods[i];
     const bool square = p.y == nullptr;
@@ -925,67 +911,37 @@ int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
     if (!p.out || (p.nx && !p.x)) return fail(HG_ERR_ARG, "product %zu: null pointer", i);
     if (p.nout < size) return fail(HG_ERR_ARG, "product %zu: nout = %zu cannot hold %llu limbs", i, p.nout,
                                    (unsigned long long)size);
-    if (p.nx == 0 || (!square && p.ny == 0)) {
-      zeros.push_back({0, square, i});
-      continue;
+    if (p.nx && (square || p.ny)) {
+      int rc = check_len(ilog2_ceil(size));
+      if (rc) return rc;
     }
-    const int L = ilog2_ceil(size);
-    int rc = check_len(L);
-    if (rc) return rc;
-    items.push_back({L, square, i});
+    out.push_back(ProductDesc{p.x, p.y, p.nx, square ? p.nx : p.ny, p.out, p.nout});
   }
-  std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &c) {
-    return a.L != c.L ? a.L < c.L : a.square < c.square;
-  });
-  auto desc_of = [&](size_t i) {
-    const hg_product &p = prods[i];
-    return ProductDesc{p.x, p.y, p.nx, p.y ? p.ny : p.nx, p.out, p.nout};
-  };
-  for (size_t s = 0; s < items.size();) {
-    size_t e = s;
-    while (e < items.size() && items[e].L == items[s].L && items[e].square == items[s].square) ++e;
-    const int L = items[s].L;
-    const bool square = items[s].square;
-    const uint64_t N = uint64_t(1) << L;
-    const uint64_t per = static_cast<uint64_t>(square ? 1 : 2) * kPrimes * N * 8;  // workspace bytes per product
-    const uint64_t chunk = std::max<uint64_t>(1, kBatchWorkspaceCap / per);
-    for (size_t c = s; c < e; c += chunk) {
-      BatchGroup g;
-      g.L = L;
-      g.square = square;
-      g.plan = plan_passes(L);
-      g.first = b->desc.size();
-      g.nprod = std::min<uint64_t>(chunk, e - c);
-      g.flags_off = b->flag_words;
-      for (size_t k = c; k < c + g.nprod; ++k) {
-        b->desc.push_back(desc_of(items[k].i));
-        if (b->desc.back().nout > N) g.tails = true;
-      }
-      b->flag_words += carry_tiles(N) * g.nprod;
-      b->ws_words = std::max<uint64_t>(b->ws_words, per / 8 * g.nprod);
-      b->groups.push_back(g);
-    }
-    s = e;
-  }
-  b->zero_first = b->desc.size();
-  b->nzero = zeros.size();
-  for (const Item &z : zeros) b->desc.push_back(desc_of(z.i));
-  Context &c = g_ctx;
-  if (!b->desc.empty()) {
-    HG_CUDA(b->d_desc.ensure(b->desc.size() * sizeof(ProductDesc)), "batch descriptors");
-    HG_CUDA(cudaMemcpy(b->d_desc.p, b->desc.data(), b->desc.size() * sizeof(ProductDesc), cudaMemcpyHostToDevice),
+  return HG_OK;
+}
+
+int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
+  if (!out) return fail(HG_ERR_ARG, "null pointer");
+  *out = nullptr;
+  std::vector<ProductDesc> items;
+  int rc = product_descs(prods, n, items);
+  if (rc) return rc;
+  std::unique_ptr<hg_batch> b(new hg_batch());
+  if ((rc = plan_batch(items.data(), items.size(), kBatchWorkspaceCap, b->bp))) return rc;
+  const BatchPlan &bp = b->bp;
+  if (!bp.desc.empty()) {
+    HG_CUDA(b->d_desc.ensure(bp.desc.size() * sizeof(ProductDesc)), "batch descriptors");
+    HG_CUDA(cudaMemcpy(b->d_desc.p, bp.desc.data(), bp.desc.size() * sizeof(ProductDesc), cudaMemcpyHostToDevice),
             "batch descriptors upload");
   }
-  if (b->ws_words) HG_CUDA(b->ws.ensure(b->ws_words * 8), "batch workspace");
-  if (b->flag_words) HG_CUDA(b->flags.ensure(b->flag_words * 8), "batch scan flags");
-  HG_CUDA(b->tickets.ensure(std::max<size_t>(1, b->groups.size()) * 8), "batch tickets");
-  (void)c;
+  if (bp.ws_words) HG_CUDA(b->ws.ensure(bp.ws_words * 8), "batch workspace");
+  if (bp.flag_words) HG_CUDA(b->flags.ensure(bp.flag_words * 8), "batch scan flags");
+  HG_CUDA(b->tickets.ensure(std::max<size_t>(1, bp.groups.size()) * 8), "batch tickets");
   if (flags & HG_BATCH_AUTOTUNE) {
-    int rc = batch_autotune(b.get());
-    if (rc) return rc;
+    if ((rc = batch_autotune(b.get()))) return rc;
   } else {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    for (BatchGroup &g : b->groups) {
+    for (BatchGroup &g : b->bp.groups) {
       auto it = g_tuned.find(std::make_tuple(g.L, g.square, g.nprod));
       if (it != g_tuned.end()) g.plan = it->second;
     }
@@ -996,17 +952,106 @@ int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
 
 int batch_run(hg_batch *b, cudaStream_t st) {
   if (!b) return fail(HG_ERR_ARG, "null batch");
-  int rc = batch_clear_scan(b, st);
-  if (rc) return rc;
-  if (b->nzero)
-    HG_CUDA(launch_zero_tails(static_cast<const ProductDesc *>(b->d_desc.p) + b->zero_first, b->nzero, 0, st),
-            "zero products");
-  for (size_t gi = 0; gi < b->groups.size(); ++gi)
-    if ((rc = run_group(b, gi, b->groups[gi].plan, st))) return rc;
-  return HG_OK;
+  return enqueue_batch(b->bp, batch_bufs(b), st);
 }
 
 }  // namespace
+
+uint64_t product_workspace_bytes(uint64_t nx, uint64_t ny, bool square) {
+  if (nx == 0 || (!square && ny == 0)) return 0;
+  const uint64_t N = uint64_t(1) << ilog2_ceil(square ? 2 * nx : nx + ny);
+  return static_cast<uint64_t>(square ? 1 : 2) * kPrimes * N * 8;
+}
+
+int plan_batch(const ProductDesc *items, size_t n, uint64_t ws_cap_bytes, BatchPlan &bp) {
+  bp = BatchPlan();
+  struct Item {
+    int L;
+    bool square;
+    size_t i;
+  };
+  std::vector<Item> live;
+  std::vector<size_t> zeros;
+  live.reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    const ProductDesc &p = items[i];
+    const bool square = p.y == nullptr;
+    if (p.nx == 0 || p.ny == 0) {
+      zeros.push_back(i);
+      continue;
+    }
+    live.push_back({ilog2_ceil(p.nx + p.ny), square, i});
+  }
+  std::stable_sort(live.begin(), live.end(), [](const Item &a, const Item &c) {
+    return a.L != c.L ? a.L < c.L : a.square < c.square;
+  });
+  bp.desc.reserve(n);
+  for (size_t s = 0; s < live.size();) {
+    size_t e = s;
+    while (e < live.size() && live[e].L == live[s].L && live[e].square == live[s].square) ++e;
+    const int L = live[s].L;
+    const bool square = live[s].square;
+    const uint64_t N = uint64_t(1) << L;
+    const uint64_t per = static_cast<uint64_t>(square ? 1 : 2) * kPrimes * N * 8;
+    if (per > ws_cap_bytes)
+      return fail(HG_ERR_ARG, "a 2^%d-point product needs %llu workspace bytes, more than the %llu available", L,
+                  (unsigned long long)per, (unsigned long long)ws_cap_bytes);
+    const uint64_t chunk = std::max<uint64_t>(1, ws_cap_bytes / per);
+    for (size_t c = s; c < e; c += chunk) {
+      BatchGroup g;
+      g.L = L;
+      g.square = square;
+      g.plan = plan_passes(L);
+      g.first = bp.desc.size();
+      g.nprod = std::min<uint64_t>(chunk, e - c);
+      g.flags_off = bp.flag_words;
+      for (size_t k = c; k < c + g.nprod; ++k) {
+        bp.desc.push_back(items[live[k].i]);
+        if (bp.desc.back().nout > N) g.tails = true;
+      }
+      bp.flag_words += carry_tiles(N) * g.nprod;
+      bp.ws_words = std::max<uint64_t>(bp.ws_words, per / 8 * g.nprod);
+      bp.groups.push_back(std::move(g));
+    }
+    s = e;
+  }
+  bp.zero_first = bp.desc.size();
+  bp.nzero = zeros.size();
+  for (size_t z : zeros) bp.desc.push_back(items[z]);
+  return HG_OK;
+}
+
+int enqueue_batch(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) {
+  int rc = batch_clear_scan(bp, bb, st);
+  if (rc) return rc;
+  if (bp.nzero) HG_CUDA(launch_zero_tails(bb.desc + bp.zero_first, bp.nzero, 0, st), "zero products");
+  for (size_t gi = 0; gi < bp.groups.size(); ++gi)
+    if ((rc = run_group(bp.groups[gi], gi, bb, bp.groups[gi].plan, st))) return rc;
+  return HG_OK;
+}
+
+std::recursive_mutex &lib_mutex() { return g_ctx.mu; }
+bool lib_ready() { return g_ctx.ready; }
+int lib_device() { return g_ctx.device; }
+
+int lib_fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  return code;
+}
+
+int lib_cuda_fail(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+
+namespace {
+std::atomic<int> g_services{0};
+}  // namespace
+
+void lib_service_count(int delta) { g_services += delta; }
+
 }  // namespace hg
 
 using namespace hg;
@@ -1060,6 +1105,7 @@ int hg_shutdown(void) {
   std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
   Context &c = g_ctx;
   if (!c.ready) return HG_OK;
+  if (g_services.load() > 0) return fail(HG_ERR_ARG, "close every multiply service before hg_shutdown");
   cudaDeviceSynchronize();
   c.A.release();
   c.B.release();

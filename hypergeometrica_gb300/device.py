@@ -113,3 +113,84 @@ def mul_batch(items, stream=None) -> None:
     """One-shot batch (hg_mul_batch_device): items are (x, y_or_None, out)."""
     arr = _products(items)
     check(load().hg_mul_batch_device(arr, len(items), _stream(stream)))
+
+
+# numpy view of hg_product records (six 64-bit fields), for bulk submission
+PRODUCT_FIELDS = ("x", "nx", "y", "ny", "out", "nout")
+
+
+def product_records(x_ptr, nx, y_ptr, ny, out_ptr, nout):
+    """An (n, 6) uint64 array laid out as hg_product[n] from equal-length
+    arrays of device addresses and sizes (y_ptr 0 squares x)."""
+    import numpy as np
+
+    cols = [np.asarray(c, dtype=np.uint64) for c in (x_ptr, nx, y_ptr, ny, out_ptr, nout)]
+    return np.ascontiguousarray(np.stack(cols, axis=1))
+
+
+class Service:
+    """The device-resident multiply service (hg_svc_*): products on device
+    memory, continuous batching on `slots` streams, admission by workspace."""
+
+    def __init__(self, workspace_bytes: int = 0, slots: int = 2, max_batch: int = 0):
+        import ctypes
+
+        h = ctypes.c_void_p()
+        check(load().hg_svc_open(workspace_bytes, slots, max_batch, ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, items) -> list[int]:
+        """Queue (x, y_or_None, out[, nx, ny]) tensor tuples; returns their tickets."""
+        arr = _products(items)
+        return self._submit_ptr(arr, len(items))
+
+    def submit_records(self, rec) -> range:
+        """Queue an (n, 6) uint64 hg_product record array (product_records)."""
+        import ctypes
+
+        from ._lib import HgProduct
+
+        n = rec.shape[0]
+        return self._submit_ptr(rec.ctypes.data_as(ctypes.POINTER(HgProduct)), n)
+
+    def _submit_ptr(self, arr, n):
+        import ctypes
+
+        first = ctypes.c_uint64()
+        check(load().hg_svc_submit(self._h, arr, n, ctypes.byref(first)))
+        return range(first.value, first.value + n)
+
+    def status(self, ticket: int) -> int:
+        return load().hg_svc_status(self._h, ticket)
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> None:
+        check(load().hg_svc_wait(self._h, ticket, timeout))
+
+    def wait_all(self, timeout: float = -1.0) -> None:
+        check(load().hg_svc_wait_all(self._h, timeout))
+
+    def stats(self, reset: bool = False) -> dict:
+        import ctypes
+
+        from ._lib import HgSvcStats
+
+        st = HgSvcStats()
+        check(load().hg_svc_stats(self._h, ctypes.byref(st), 1 if reset else 0))
+        return {name: getattr(st, name) for name, _ in HgSvcStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            h, self._h = self._h, None
+            check(load().hg_svc_close(h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

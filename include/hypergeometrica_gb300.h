@@ -180,6 +180,53 @@ int hg_batch_destroy(hg_batch *batch);
  * run on stream, wait, destroy. */
 int hg_mul_batch_device(const hg_product *prods, size_t n, void *stream);
 
+/* ---- device-resident multiply service ---------------------------------- */
+
+/* Replaces the one-product-at-a-time mpz-* calls that binary-split / combine
+ * (src/binary-splitting.lisp:100-133) and the MPD Newton steps
+ * (src/mpd-reciprocal.lisp:27-73, src/mpd-sqrt.lisp:40-90) make.  Operands
+ * and results stay in device memory; a worker thread batches the submitted
+ * products (continuous batching: products submitted while batches run join
+ * the next batch as a slot frees up) and admits them by free workspace. */
+typedef struct hg_svc hg_svc;
+
+typedef struct hg_svc_report {
+    uint64_t submitted, completed, failed, batches;
+    uint64_t pending, in_flight;          /* at the time of the call             */
+    uint64_t peak_batch_products;         /* since the last reset                */
+    uint64_t peak_batch_workspace_bytes;  /* since the last reset                */
+    uint64_t slot_workspace_bytes;
+    uint64_t latency_samples;             /* products completed since the reset  */
+    int slots;
+    double p50_us, p99_us, mean_us, max_us; /* submit-to-completion latency     */
+    double products_per_s;  /* completed since the reset / (last completion - first submission) */
+} hg_svc_report;
+
+/* Open a service with `slots` CUDA streams (1..8) sharing workspace_bytes of
+ * device memory (0: half the free memory, at most 8 GiB), allocated now;
+ * max_batch products per batch (0: 2^20).  Needs hg_init; close every
+ * service before hg_shutdown. */
+int hg_svc_open(size_t workspace_bytes, int slots, size_t max_batch, hg_svc **svc);
+/* Queue n products (device pointers, as hg_product); they get the tickets
+ * *first_ticket .. *first_ticket + n - 1.  All are checked before any is
+ * queued: a product whose transform workspace exceeds one slot is
+ * HG_ERR_ARG.  The service's streams are not ordered after the caller's:
+ * the operands must be complete in device memory when this is called (for
+ * example, synchronise the stream that wrote them), and operands and outputs
+ * must stay valid until the product is done.  Thread-safe. */
+int hg_svc_submit(hg_svc *svc, const hg_product *prods, size_t n, uint64_t *first_ticket);
+/* 1 done, 0 pending, < 0 the HG_ERR_* code the product failed with. */
+int hg_svc_status(hg_svc *svc, uint64_t ticket);
+/* Wait for one product (timeout_s < 0: no limit); HG_ERR_TIMEOUT when the
+ * time runs out first. */
+int hg_svc_wait(hg_svc *svc, uint64_t ticket, double timeout_s);
+/* Wait for every product submitted so far. */
+int hg_svc_wait_all(hg_svc *svc, double timeout_s);
+/* Counters and latency percentiles; reset != 0 starts a new latency window. */
+int hg_svc_stats(hg_svc *svc, hg_svc_report *out, int reset);
+/* Finish the queued products, stop the worker, free the service. */
+int hg_svc_close(hg_svc *svc);
+
 /* ---- spectra (parity hooks) -------------------------------------------- */
 
 /* ntt-forward (src/number-theoretic-transform.lisp:40-90) in place on n
