@@ -180,6 +180,33 @@ int hg_batch_destroy(hg_batch *batch);
  * run on stream, wait, destroy. */
 int hg_mul_batch_device(const hg_product *prods, size_t n, void *stream);
 
+/* ---- sums and sizes of many device integers ---------------------------- */
+
+/* One signed sum: out = sa*|a| + sb*|b| (magnitude), nout >= max(na, nb) + 1. */
+typedef struct hg_sum {
+    const uint64_t *a; /* device limbs */
+    size_t na;
+    const uint64_t *b; /* device limbs */
+    size_t nb;
+    uint64_t *out;     /* device limbs; written up to nout */
+    size_t nout;
+    int64_t sa, sb;    /* +1 or -1 */
+} hg_sum;
+
+/* mpz-+ (src/mpz-ram.lisp:292-306) on n pairs at once: result[2k] receives
+ * the sign of sum k (+1 for zero) and result[2k + 1] its length without high
+ * zero limbs (device int64 array of 2n entries). */
+int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *stream);
+
+typedef struct hg_vec {
+    const uint64_t *p; /* device limbs */
+    size_t n;
+} hg_vec;
+
+/* mpz-size (vec-digit-length*, src/vec.lisp:218-229) of n device integers:
+ * sizes[k] = length of vecs[k] without high zero limbs (device array). */
+int hg_trim_batch_device(const hg_vec *vecs, size_t n, uint64_t *sizes, void *stream);
+
 /* ---- device-resident multiply service ---------------------------------- */
 
 /* Replaces the one-product-at-a-time mpz-* calls that binary-split / combine

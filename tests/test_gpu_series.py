@@ -1,0 +1,147 @@
+"""Binary splitting on the GPU (series.binary_split) and the batched signed
+sums and trims it is built from, against the oracle.
+
+Integers throughout: every comparison is exact.  Small and medium ranges
+compare P, Q, B, R with the oracle's recursion on Python integers; the
+Chudnovsky ranges of 2^22 and 2^24-bit pi compare them modulo primes with
+the oracle's closed forms (a size-independent check).
+"""
+
+import numpy as np
+import pytest
+
+import series_oracle as O
+from hypergeometrica_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _as_int(limbs, sign=1):
+    from hypergeometrica_gb300.mpz import int_from_digits
+
+    v = int_from_digits(limbs)
+    return -v if sign < 0 else v
+
+
+def _dev(a):
+    import torch
+
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    if a.size == 0:
+        return torch.zeros(1, dtype=torch.int64, device="cuda"), 0
+    return torch.from_numpy(a.view(np.int64).copy()).cuda(), a.size
+
+
+def _cases():
+    rng = np.random.default_rng(5)
+    out = []
+    sizes = [0, 1, 2, 7, 2047, 2048, 2049, 5000, 20000]
+    for k in range(60):
+        na = int(rng.choice(sizes))
+        nb = int(rng.choice(sizes))
+        a = W.limbs(10 * k + 1, na)
+        b = W.limbs(10 * k + 2, nb)
+        kind = k % 6
+        if kind == 1:  # long carry chains
+            a = np.full(na, np.uint64(2**64 - 1))
+            b = np.zeros(nb, dtype=np.uint64)
+            if nb:
+                b[0] = 1
+        elif kind == 2 and na:  # equal magnitudes
+            b = a.copy()
+        elif kind == 3 and na and nb:  # equal tops, differ low
+            b = a.copy()
+            b[0] ^= np.uint64(1)
+        elif kind == 4 and na > 1:  # borrow chains: a = 2^(64(n-1)), b = 1
+            a = np.zeros(na, dtype=np.uint64)
+            a[-1] = 1
+            b = np.ones(1, dtype=np.uint64)
+        signs = [(1, 1), (1, -1), (-1, 1), (-1, -1)][k % 4]
+        out.append((a, b, *signs))
+    return out
+
+
+def test_signed_sums_and_trims(hg):
+    import torch
+
+    from hypergeometrica_gb300 import series as S
+
+    cases = _cases()
+    keep, rec, want = [], [], []
+    for a, b, sa, sb in cases:
+        ta, na = _dev(a)
+        tb, nb = _dev(b)
+        nout = max(na, nb) + 1 + 3
+        out = torch.full((nout,), -1, dtype=torch.int64, device="cuda")
+        keep += [ta, tb, out]
+        rec.append([ta.data_ptr(), na, tb.data_ptr(), nb, out.data_ptr(), nout,
+                    np.int64(sa).view(np.uint64), np.int64(sb).view(np.uint64)])
+        want.append(sa * _as_int(a) + sb * _as_int(b))
+    torch.cuda.synchronize()
+    res = S._sum_records(np.array(rec, dtype=np.uint64))
+    for k, (v, (sg, size)) in enumerate(zip(want, res)):
+        out = keep[3 * k + 2].cpu().numpy().view(np.uint64)
+        assert size == (abs(v).bit_length() + 63) // 64, k
+        assert sg == (-1 if v < 0 else 1), k
+        assert _as_int(out) == abs(v), k  # every limb up to nout written
+    # trims of the outputs, with their written lengths
+    tr = S.trim_sizes([(keep[3 * k + 2], keep[3 * k + 2].numel()) for k in range(len(cases))])
+    assert list(tr) == [int(s) for _, s in res]
+
+
+SERIES = {
+    "chudnovsky": ("make_chudnovsky_series", O.chudnovsky_series()),
+    "e": ("make_e_series", O.e_series()),
+    "ramanujan": ("make_ramanujan_series", O.ramanujan_series()),
+    "catalan": ("make_catalan_series", O.catalan_series()),
+    "apery": ("make_apery_series", O.apery_series()),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SERIES))
+@pytest.mark.parametrize("lo,hi", [(0, 1), (0, 2), (0, 3), (0, 8), (5, 40), (0, 333)])
+def test_binary_split_matches_oracle(hg, name, lo, hi):
+    from hypergeometrica_gb300 import series as S
+
+    maker, ser = SERIES[name]
+    part = S.binary_split(getattr(S, maker)(), lo, hi)
+    want = O.binary_split(ser, lo, hi)
+    got = (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int())
+    assert got == want
+
+
+def test_exp_series_with_service(hg):
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import series as S
+
+    with D.Service(workspace_bytes=64 << 20, slots=2) as svc:
+        part = S.binary_split(S.make_exp_series("-2/7"), 0, 150, service=svc)
+        den = S.partial_denominator(part, svc)
+    P, Q, B, R = O.binary_split(O.exp_series("-2/7"), 0, 150)
+    assert (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int()) == (P, Q, B, R)
+    assert den.to_int() == B * Q
+
+
+@pytest.mark.parametrize("bits", [1 << 12, 1 << 16, 1 << 20])
+def test_chudnovsky_partials_exact(hg, bits):
+    """The partials mpd-pi splits for a 2^12, 2^16 and 2^20-bit pi, exactly."""
+    from hypergeometrica_gb300 import series as S
+
+    n = S.chudnovsky_terms(bits)
+    part = S.binary_split(S.make_chudnovsky_series(), 0, n)
+    want = O.binary_split(O.chudnovsky_series(), 0, n)
+    assert (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int()) == want
+
+
+@pytest.mark.parametrize("bits", [1 << 22, 1 << 24])
+def test_chudnovsky_partials_residues(hg, bits):
+    """The 2^22 and 2^24-bit pi partials modulo three primes."""
+    from hypergeometrica_gb300 import series as S
+
+    n = S.chudnovsky_terms(bits)
+    part = S.binary_split(S.make_chudnovsky_series(), 0, n)
+    vals = [x.to_int() for x in (part.p, part.q, part.b, part.r)]
+    for m in ((1 << 61) - 1, 2305843009213693921, 998244353):
+        assert tuple(v % m for v in vals) == O.residues(O.chudnovsky_series(), 0, n, m)
+    # Q is the product of q(k) = k^3 640320^3 / 24: a check of its length too
+    assert part.q.size == (vals[1].bit_length() + 63) // 64
