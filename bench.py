@@ -308,6 +308,71 @@ def run_batched(stream, steps: int) -> dict:
     }
 
 
+MPD_BITS = (1 << 22, 1 << 24, 1 << 26)
+MPD_EXACT_BITS = 10000
+
+
+def run_mpd_pi(cpu: bool) -> dict:
+    """Chudnovsky pi/10 through the device-resident multiply service.
+
+    At 2^22, 2^24 and 2^26 bits: binary splitting (partials in HBM, every
+    product through the service) and Newton steps kept at working precision
+    (the reference never truncates, so its own result at these sizes would
+    need terabytes; this variant is labelled and is not its mantissa).  The
+    largest run's partials are checked modulo a prime against the oracle's
+    closed forms.  At 10^4 bits the untruncated, reference-identical mpd_pi
+    runs on the GPU and on the CPU oracle; the two must be bit-identical."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import mpd as G
+    from hypergeometrica_gb300 import series as S
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    out = {"metric": "mpd-pi wall time", "unit": "s", "runs": []}
+    with D.Service(workspace_bytes=2 << 30, slots=2) as svc:
+        G.mpd_pi_truncated(1 << 12, service=svc)  # warm the kernels and the service
+        for bits in MPD_BITS:
+            svc.stats(reset=True)
+            t = {}
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            G.mpd_pi_truncated(bits, service=svc, timings=t)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            st = svc.stats()
+            out["runs"].append({
+                "bits": bits, "variant": "truncated Newton (not the reference's untruncated mantissa)",
+                "wall_s": wall, **t,
+                "service": {k: st[k] for k in ("completed", "batches", "p50_us", "p99_us", "mean_us",
+                                               "products_per_s", "peak_batch_products")}})
+        import series_oracle as SO
+
+        bits = MPD_BITS[-1]
+        n = S.chudnovsky_terms(bits)
+        part = S.binary_split(S.make_chudnovsky_series(), 0, n, service=svc)
+        m = (1 << 61) - 1
+        got = tuple(x.to_int() % m for x in (part.p, part.q, part.b, part.r))
+        out["partials_check"] = {"bits": bits, "terms": n, "modulus": "2^61-1",
+                                 "match": got == SO.residues(SO.chudnovsky_series(), 0, n, m)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = G.mpd_pi(MPD_EXACT_BITS)
+    torch.cuda.synchronize()
+    exact = {"bits": MPD_EXACT_BITS, "variant": "untruncated, the reference's mpd-pi",
+             "gpu_s": time.perf_counter() - t0, "mantissa_limbs": x.mantissa.size}
+    if cpu:
+        import mpd_oracle as MO
+
+        t0 = time.perf_counter()
+        ref = MO.mpd_pi(MPD_EXACT_BITS)
+        exact["cpu_oracle_s"] = time.perf_counter() - t0
+        exact["bit_identical"] = x.to_pair() == (ref.m, ref.e)
+    out["exact"] = exact
+    out["correct"] = out["partials_check"]["match"] and exact.get("bit_identical", True)
+    return out
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -431,6 +496,9 @@ def run_ours(args) -> None:
     if not args.no_batched:
         line["batched"] = run_batched(stream, args.steps)
         line["correct"] = line["correct"] and line["batched"]["correct"]
+    if not args.no_mpd and ws == 1:
+        line["mpd_pi"] = run_mpd_pi(cpu=not args.no_cpu_baseline)
+        line["correct"] = line["correct"] and line["mpd_pi"]["correct"]
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cores, model = _cpu_info()
         threads = min(6, cores)
@@ -454,6 +522,7 @@ def main():
     ap.add_argument("--log-size", type=int, default=LOG_SIZE, help="log2 limbs per operand (default 24)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 4096-pair batched-products measurement")
+    ap.add_argument("--no-mpd", action="store_true", help="skip the mpd-pi measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

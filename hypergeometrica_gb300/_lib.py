@@ -58,6 +58,13 @@ class HgProduct(ctypes.Structure):
 HG_BATCH_AUTOTUNE = 1
 
 
+class HgPoly(ctypes.Structure):
+    """hg_poly: an integer polynomial with an optional value at 0."""
+
+    _fields_ = [("coef", ctypes.c_int64 * 8), ("degree", ctypes.c_int32), ("has_zero_value", ctypes.c_int32),
+                ("zero_value", ctypes.c_int64)]
+
+
 class HgSvcStats(ctypes.Structure):
     """hg_svc_report: counters and submit-to-completion latency of a service."""
 
@@ -92,6 +99,7 @@ SIGNATURES = {
     "hg_mul_batch_device": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, _vp]),
     "hg_add_batch_device": (ctypes.c_int, [_vp, _sz, _vp, _vp]),
     "hg_trim_batch_device": (ctypes.c_int, [_vp, _sz, _vp, _vp]),
+    "hg_series_leaves_device": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp]),
     "hg_svc_open": (ctypes.c_int, [_sz, ctypes.c_int, _sz, ctypes.POINTER(_vp)]),
     "hg_svc_submit": (ctypes.c_int, [_vp, ctypes.POINTER(HgProduct), _sz, ctypes.POINTER(ctypes.c_uint64)]),
     "hg_svc_status": (ctypes.c_int, [_vp, ctypes.c_uint64]),

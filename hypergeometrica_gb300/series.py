@@ -43,10 +43,50 @@ def one(n: int) -> int:
 
 @dataclass(frozen=True)
 class Series:
+    """a, b, p, q as functions of k; `poly` optionally gives the same four as
+    integer polynomials, ((c0, c1, ...), value at k = 0 or None) each, so that
+    the base cases can be evaluated on the device."""
+
     a: Callable[[int], int] = one
     b: Callable[[int], int] = one
     p: Callable[[int], int] = one
     q: Callable[[int], int] = one
+    poly: tuple | None = None
+
+
+def _poly_series(a, b, p, q) -> Series:
+    """A Series from four (coefficients low to high, value at 0 or None) pairs."""
+
+    def fn(spec):
+        coefs, zero = spec
+
+        def f(n):
+            if n == 0 and zero is not None:
+                return zero
+            acc = 0
+            for c in reversed(coefs):
+                acc = acc * n + c
+            return acc
+
+        return f
+
+    return Series(a=fn(a), b=fn(b), p=fn(p), q=fn(q), poly=(a, b, p, q))
+
+
+def _poly_bits(spec, n_max: int) -> int:
+    coefs, zero = spec
+    bound = sum(abs(c) * n_max ** i for i, c in enumerate(coefs))
+    return max(bound.bit_length(), abs(zero or 0).bit_length())
+
+
+def _device_leaves_fit(series: Series, upper: int) -> bool:
+    if series.poly is None or upper > (1 << 62):
+        return False
+    for coefs, zero in series.poly:
+        if len(coefs) > 8 or any(abs(c) >= 1 << 63 for c in coefs) or abs(zero or 0) >= 1 << 63:
+            return False
+    bits = [_poly_bits(spec, max(1, upper - 1)) for spec in series.poly]
+    return max(bits) <= 254 and bits[2] + bits[0] <= 254
 
 
 class DeviceInt:
@@ -224,24 +264,35 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
     lo, hi, left, right, height = _tree(lower, upper)
     nn = lo.size
     leaves = np.flatnonzero(left < 0)
-    ks = lo[leaves].tolist()
-    # binary-split-base-case=1 (:102-110): P = p(k), Q = q(k), B = b(k), R = p(k) a(k)
-    pv = [series.p(k) for k in ks]
-    vals = [pv, [series.q(k) for k in ks], [series.b(k) for k in ks],
-            [pk * series.a(k) for pk, k in zip(pv, ks)]]
     ptr = np.zeros((4, nn), dtype=np.uint64)
     size = np.zeros((4, nn), dtype=np.int64)
     sign = np.ones((4, nn), dtype=np.int64)
-    base_off = 0
-    packed = [_pack(v) for v in vals]
-    leaf_limbs = sum(int(pk[2].sum()) for pk in packed)
-    arena0 = torch.from_numpy(np.concatenate([pk[1].reshape(-1) for pk in packed]).view(np.int64)).cuda()
-    base = arena0.data_ptr()
-    for j, (sg, limbs, sz, w) in enumerate(packed):
-        ptr[j, leaves] = base + 8 * (base_off + w * np.arange(leaves.size, dtype=np.uint64))
-        size[j, leaves] = sz
-        sign[j, leaves] = sg
-        base_off += w * leaves.size
+    # binary-split-base-case=1 (:102-110): P = p(k), Q = q(k), B = b(k), R = p(k) a(k)
+    if _device_leaves_fit(series, upper):
+        arena0, ss = _device_leaves(series, lower, upper)
+        base = arena0.data_ptr()
+        count = upper - lower
+        kidx = (lo[leaves] - lower).astype(np.uint64)
+        for j in range(4):
+            ptr[j, leaves] = base + 8 * 4 * (np.uint64(j * count) + kidx)
+            sign[j, leaves] = ss[j, kidx, 0]
+            size[j, leaves] = ss[j, kidx, 1]
+        leaf_limbs = int(size[:, leaves].sum())
+    else:
+        ks = lo[leaves].tolist()
+        pv = [series.p(k) for k in ks]
+        vals = [pv, [series.q(k) for k in ks], [series.b(k) for k in ks],
+                [pk * series.a(k) for pk, k in zip(pv, ks)]]
+        base_off = 0
+        packed = [_pack(v) for v in vals]
+        leaf_limbs = sum(int(pk[2].sum()) for pk in packed)
+        arena0 = torch.from_numpy(np.concatenate([pk[1].reshape(-1) for pk in packed]).view(np.int64)).cuda()
+        base = arena0.data_ptr()
+        for j, (sg, limbs, sz, w) in enumerate(packed):
+            ptr[j, leaves] = base + 8 * (base_off + w * np.arange(leaves.size, dtype=np.uint64))
+            size[j, leaves] = sz
+            sign[j, leaves] = sg
+            base_off += w * leaves.size
     root_off = None  # the root's arena and the offsets of its P, Q, B, R
     arenas = {0: arena0}
     del arena0
@@ -320,6 +371,27 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
     return Partial(lower, upper, dev_int(0), dev_int(1), dev_int(2), dev_int(3))
 
 
+def _device_leaves(series: Series, lower: int, upper: int):
+    """hg_series_leaves_device: ((4 * count * 4) limb arena, (4, count, 2) signs and sizes)."""
+    import torch
+
+    from ._lib import HgPoly
+
+    polys = (HgPoly * 4)()
+    for j, (coefs, zero) in enumerate(series.poly):
+        for i, c in enumerate(coefs):
+            polys[j].coef[i] = c
+        polys[j].degree = len(coefs) - 1
+        polys[j].has_zero_value = 0 if zero is None else 1
+        polys[j].zero_value = 0 if zero is None else zero
+    count = upper - lower
+    limbs = torch.empty(16 * count, dtype=torch.int64, device="cuda")
+    ss = torch.empty(8 * count, dtype=torch.int64, device="cuda")
+    st = torch.cuda.current_stream()
+    check(load().hg_series_leaves_device(polys, lower, count, limbs.data_ptr(), ss.data_ptr(), st.cuda_stream))
+    return limbs, ss.cpu().numpy().reshape(4, count, 2)
+
+
 def _offsets(sizes_list):
     """Start offsets of consecutive blocks: sizes_list[0] for every node, then
     sizes_list[1], ..."""
@@ -339,31 +411,29 @@ def make_exp_series(x) -> Series:
     """make-exp-series (src/binary-splitting.lisp:147-155): e^x for rational x."""
     x = Fraction(x)
     num, den = x.numerator, x.denominator
-    return Series(p=lambda n: 1 if n == 0 else num, q=lambda n: 1 if n == 0 else n * den)
+    return _poly_series(a=((1,), None), b=((1,), None), p=((num,), 1), q=((0, den), 1))
 
 
 def make_e_series() -> Series:
     """make-e-series (:157-161)."""
-    return Series(q=lambda n: 1 if n == 0 else n)
+    return _poly_series(a=((1,), None), b=((1,), None), p=((1,), None), q=((0, 1), 1))
 
 
 def make_ramanujan_series() -> Series:
-    """make-ramanujan-series (:174-193)."""
-    c4_8 = 396 ** 4 // 8
-    return Series(a=lambda n: 1103 + n * 26390,
-                  p=lambda n: 1 if n == 0 else -3 + n * (22 + n * (-48 + n * 32)),
-                  q=lambda n: 1 if n == 0 else n ** 3 * c4_8)
+    """make-ramanujan-series (:174-193): p = 32k^3 - 48k^2 + 22k - 3, q = k^3 396^4 / 8."""
+    return _poly_series(a=((1103, 26390), None), b=((1,), None), p=((-3, 22, -48, 32), 1),
+                        q=((0, 0, 0, 396 ** 4 // 8), 1))
 
 
 def make_catalan_series() -> Series:
     """make-catalan-series (:213-223)."""
-    return Series(b=lambda n: 1 + 2 * n, p=lambda n: 1 if n == 0 else n, q=lambda n: 1 if n == 0 else 2 + 4 * n)
+    return _poly_series(a=((1,), None), b=((1, 2), None), p=((0, 1), 1), q=((2, 4), 1))
 
 
 def make_apery_series() -> Series:
-    """make-apery-series (:226-231)."""
-    return Series(a=lambda n: 77 + n * (250 + n * 205), b=lambda n: 2,
-                  p=lambda n: 1 if n == 0 else -(n ** 5), q=lambda n: 32 * (1 + 2 * n) ** 5)
+    """make-apery-series (:226-231): q = 32 (2k + 1)^5 expanded."""
+    return _poly_series(a=((77, 250, 205), None), b=((2,), None), p=((0, 0, 0, 0, 0, -1), 1),
+                        q=((32, 320, 1280, 2560, 2560, 1024), None))
 
 
 CHUD_A, CHUD_B, CHUD_C = 13591409, 545140134, 640320
@@ -373,13 +443,11 @@ CHUD_DECIMALS_PER_TERM = math.log10(151931373056000)
 
 
 def make_chudnovsky_series() -> Series:
-    """make-chudnovsky-series (src/pi.lisp:24-43), for pi/10."""
-    c3_24 = CHUD_C ** 3 // 24
-    b = 1 * (8 * CHUD_C) // 12  # (* (denominator 10) (/ (* 8 +chud-c+) 12))
-    return Series(a=lambda n: CHUD_A * CHUD_PREFACTOR + n * (CHUD_B * CHUD_PREFACTOR),
-                  b=lambda n: b,
-                  p=lambda n: 1 if n == 0 else 5 + n * (-46 + n * (108 + n * -72)),
-                  q=lambda n: 1 if n == 0 else n ** 3 * c3_24)
+    """make-chudnovsky-series (src/pi.lisp:24-43), for pi/10: a = 10 (A + B k),
+    b = 8 C / 12, p = -72k^3 + 108k^2 - 46k + 5, q = k^3 C^3 / 24."""
+    return _poly_series(a=((CHUD_A * CHUD_PREFACTOR, CHUD_B * CHUD_PREFACTOR), None),
+                        b=(((8 * CHUD_C) // 12,), None), p=((5, -46, 108, -72), 1),
+                        q=((0, 0, 0, CHUD_C ** 3 // 24), 1))
 
 
 def chudnovsky_terms(prec_bits: int) -> int:

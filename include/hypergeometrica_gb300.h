@@ -207,6 +207,28 @@ typedef struct hg_vec {
  * sizes[k] = length of vecs[k] without high zero limbs (device array). */
 int hg_trim_batch_device(const hg_vec *vecs, size_t n, uint64_t *sizes, void *stream);
 
+/* ---- binary-splitting base cases -------------------------------------- */
+
+/* An integer polynomial coef[0] + coef[1] k + ... + coef[degree] k^degree
+ * (degree 0..7); when has_zero_value is nonzero its value at k = 0 is
+ * zero_value instead (the reference's "(if (zerop n) 1 ...)"). */
+typedef struct hg_poly {
+    int64_t coef[8];
+    int32_t degree;
+    int32_t has_zero_value;
+    int64_t zero_value;
+} hg_poly;
+
+/* binary-split-base-case=1 (src/binary-splitting.lisp:102-110) for the
+ * terms k = lower .. lower + count - 1 of a series whose a, b, p, q are the
+ * polynomials polys[0..3]: P = p(k), Q = q(k), B = b(k), R = p(k) a(k).
+ * Value j of term i goes to limbs[(j count + i) 4 .. + 3] (four limbs,
+ * magnitude) and sign_size[(j count + i) 2] = sign (+1 for zero),
+ * [.. + 1] = length without high zero limbs (device arrays).  Every value and
+ * R must fit in 255 bits; the caller checks the bound. */
+int hg_series_leaves_device(const hg_poly *polys, uint64_t lower, uint64_t count, uint64_t *limbs,
+                            int64_t *sign_size, void *stream);
+
 /* ---- device-resident multiply service ---------------------------------- */
 
 /* Replaces the one-product-at-a-time mpz-* calls that binary-split / combine

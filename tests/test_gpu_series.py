@@ -145,3 +145,33 @@ def test_chudnovsky_partials_residues(hg, bits):
         assert tuple(v % m for v in vals) == O.residues(O.chudnovsky_series(), 0, n, m)
     # Q is the product of q(k) = k^3 640320^3 / 24: a check of its length too
     assert part.q.size == (vals[1].bit_length() + 63) // 64
+
+
+@pytest.mark.parametrize("name", sorted(SERIES) + ["exp"])
+@pytest.mark.parametrize("lo,count", [(0, 70), (10**6, 40), ((1 << 31) - 40, 40)])
+def test_device_leaves_match_python(hg, name, lo, count):
+    """hg_series_leaves_device against the series' own functions."""
+    from hypergeometrica_gb300 import series as S
+
+    ser = S.make_exp_series("-5/3") if name == "exp" else getattr(S, SERIES[name][0])()
+    assert S._device_leaves_fit(ser, lo + count)
+    limbs, ss = S._device_leaves(ser, lo, lo + count)
+    host = limbs.cpu().numpy().view(np.uint64).reshape(4, count, 4)
+    for i in range(count):
+        k = lo + i
+        pk = ser.p(k)
+        for j, v in enumerate((pk, ser.q(k), ser.b(k), pk * ser.a(k))):
+            size = (abs(v).bit_length() + 63) // 64
+            assert ss[j, i, 1] == size and ss[j, i, 0] == (-1 if v < 0 else 1), (j, k)
+            assert _as_int(host[j, i]) == abs(v), (j, k)
+
+
+def test_python_leaves_for_a_series_without_polynomials(hg):
+    from hypergeometrica_gb300 import series as S
+
+    ser = S.Series(a=lambda n: 3 ** n - 7, b=lambda n: n + 2, p=lambda n: 1 if n == 0 else -(2 ** (n % 70)) - n,
+                   q=lambda n: 1 if n == 0 else n * n + 1)
+    assert not S._device_leaves_fit(ser, 90)
+    part = S.binary_split(ser, 0, 90)
+    want = O.binary_split((ser.a, ser.b, ser.p, ser.q), 0, 90)
+    assert (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int()) == want
