@@ -373,6 +373,28 @@ def run_mpd_pi(cpu: bool) -> dict:
     return out
 
 
+def run_expt() -> dict:
+    """9^(9^9) by mpz-expt with every partial power in device memory (the
+    x^x^x workload of the reference's published runs).  The bit length is the
+    log's known answer; the published time is the reference's own run
+    (logs/24apr21-999-ram.txt:205-226, SBCL with intrinsics and threads)."""
+    import torch
+
+    from hypergeometrica_gb300 import series as S
+
+    S.mpz_expt_device(9, 9**5)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = S.mpz_expt_device(9, 9**9)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    top = int(x.t[x.size - 1].item()) & (2**64 - 1)
+    bits = 64 * (x.size - 1) + top.bit_length()
+    return {"workload": "9^(9^9) (mpz-expt: 28 squarings + 13 products by 9, largest 2^25-point)", "wall_s": wall,
+            "bits": bits, "correct": bits == 1228093895,
+            "reference_published_s": 136.233, "reference_published_note": "logs/24apr21-999-ram.txt, other hardware"}
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -496,6 +518,9 @@ def run_ours(args) -> None:
     if not args.no_batched:
         line["batched"] = run_batched(stream, args.steps)
         line["correct"] = line["correct"] and line["batched"]["correct"]
+    if not args.no_mpd and ws == 1:
+        line["expt"] = run_expt()
+        line["correct"] = line["correct"] and line["expt"]["correct"]
     if not args.no_mpd and ws == 1:
         line["mpd_pi"] = run_mpd_pi(cpu=not args.no_cpu_baseline)
         line["correct"] = line["correct"] and line["mpd_pi"]["correct"]

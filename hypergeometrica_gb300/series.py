@@ -139,26 +139,41 @@ def partial_denominator(x: Partial, service=None) -> DeviceInt:
 
 
 def multiply(x: DeviceInt, y: DeviceInt, service=None) -> DeviceInt:
-    """mpz-* of two device integers (one product; through the service when given)."""
+    """mpz-* of two device integers (one product; through the service when
+    given).  x is y squares (mpz-square's single forward transform)."""
     import torch
 
     from . import device as D
 
+    square = x is y
     n = max(1, x.size + y.size)
     out = torch.empty(n, dtype=torch.int64, device="cuda")
     if x.size == 0 or y.size == 0:
         out.zero_()
         return DeviceInt(1, out, 0)
-    xs, ys = x.t[: x.size], y.t[: y.size]
+    xs, ys = x.t[: x.size], (None if square else y.t[: y.size])
     if service is not None:
         torch.cuda.current_stream().synchronize()
         (t,) = service.submit([(xs, ys, out)])
         service.wait(t)
+    elif square:
+        D.sqr(xs, out)
+        D.sync()
     else:
         D.mul(xs, ys, out)
         D.sync()
     sizes = trim_sizes([(out, n)])
     return DeviceInt(x.sign * y.sign, out, int(sizes[0]))
+
+
+def mpz_expt_device(a, n: int, service=None) -> DeviceInt:
+    """mpz-expt (src/multiply.lisp:77-79) with the operand and every partial
+    power in device memory: f-expt's left-to-right binary powering
+    (:51-75), squaring through mpz-square."""
+    from .mpz import f_expt
+
+    x = a if isinstance(a, DeviceInt) else DeviceInt.from_int(a)
+    return f_expt(x, n, DeviceInt.from_int(1), lambda u, v: multiply(u, v, service))
 
 
 def trim_sizes(vecs) -> np.ndarray:
