@@ -132,6 +132,8 @@ struct Context {
   unsigned long long ticket_count = 0;
   uint32_t epoch = 0;
   cudaEvent_t ws_done = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host entry points: upload of the second operand
+  cudaEvent_t copy_done = nullptr;
   bool ws_pending = false;
   std::recursive_mutex mu;
 };
@@ -275,6 +277,8 @@ int init_locked(const uint64_t *moduli, int k, int device) {
   }
   HG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream creation");
   HG_CUDA(cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming), "event creation");
+  HG_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking), "stream creation");
+  HG_CUDA(cudaEventCreateWithFlags(&c.copy_done, cudaEventDisableTiming), "event creation");
   HG_CUDA(c.misc.ensure(64), "scan state allocation");
   HG_CUDA(cudaMemset(c.misc.p, 0, 64), "scan state init");
   c.ready = true;
@@ -349,11 +353,12 @@ double pass_bytes(const PassArgs &a, int readers, int writers) {
   return bytes;
 }
 
-// The strided passes of `plan` (all but its last entry), forward in order or
-// inverse in reverse order.
-cudaError_t run_strided(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
+// Strided passes [s0, s1) of `plan` (whose last entry is the contiguous
+// pass), forward in order or inverse in reverse order.
+cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, int s0, int s1,
+                              cudaStream_t st) {
   const int np = static_cast<int>(plan.size()) - 1;
-  for (int s = 0; s < np; ++s) {
+  for (int s = s0; s < s1 && s < np; ++s) {
     const PassPlan &pp = plan[inverse ? np - 1 - s : s];
     a.logR = pp.logR;
     a.logS = pp.logS;
@@ -369,6 +374,11 @@ cudaError_t run_strided(PassArgs a, const std::vector<PassPlan> &plan, bool inve
     a.read_limbs = 0;
   }
   return cudaSuccess;
+}
+
+// All strided passes of `plan`.
+cudaError_t run_strided(const PassArgs &a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
+  return run_strided_range(a, plan, inverse, 0, static_cast<int>(plan.size()) - 1, st);
 }
 
 // The contiguous pass (the plan's last entry) in the given mode.
@@ -439,8 +449,11 @@ int check_len(int L) {
 }
 
 // |x| * |y| (or |x|^2 when y == nullptr) into out[0, nout) on device memory.
+// When y_ready is given (two operands), operand 1's limbs may still be in
+// flight: the first strided pass runs for operand 0 alone, then waits for the
+// event and runs for operand 1, so that an upload of y overlaps it.
 int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out, uint64_t nout,
-                       cudaStream_t st) {
+                       cudaStream_t st, cudaEvent_t y_ready = nullptr) {
   Context &c = g_ctx;
   const bool square = (y == nullptr);
   if (square) ny = nx;
@@ -473,7 +486,21 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   a.limbs[1] = square ? nullptr : y;
   a.nlimbs[0] = nx;
   a.nlimbs[1] = square ? 0 : ny;
-  HG_CUDA(run_strided(a, plan, false, st), "forward transform");
+  if (y_ready && !square && plan.size() > 1) {
+    PassArgs a0 = a, a1 = a, rest = a;
+    a0.nops = a1.nops = 1;
+    a1.data[0] = c.B.u64();
+    a1.limbs[0] = y;
+    a1.nlimbs[0] = ny;
+    HG_CUDA(run_strided_range(a0, plan, false, 0, 1, st), "forward transform");
+    HG_CUDA(cudaStreamWaitEvent(st, y_ready, 0), "operand upload ordering");
+    HG_CUDA(run_strided_range(a1, plan, false, 0, 1, st), "forward transform");
+    rest.limbs[0] = rest.limbs[1] = nullptr;
+    HG_CUDA(run_strided_range(rest, plan, false, 1, static_cast<int>(plan.size()) - 1, st), "forward transform");
+  } else {
+    if (y_ready) HG_CUDA(cudaStreamWaitEvent(st, y_ready, 0), "operand upload ordering");
+    HG_CUDA(run_strided(a, plan, false, st), "forward transform");
+  }
   {
     PassArgs m = a;
     if (plan.size() > 1) m.limbs[0] = m.limbs[1] = nullptr;
@@ -687,6 +714,20 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
   const uint64_t *dx = static_cast<const uint64_t *>(pinned_view(x));
   const uint64_t *dy = two ? static_cast<const uint64_t *>(pinned_view(y)) : nullptr;
   uint64_t *dout = static_cast<uint64_t *>(const_cast<void *>(pinned_view(out)));
+  // A two-operand NTT product with strided passes copies its operands over
+  // the host link instead of reading them in place: x first, then y on the
+  // copy stream while the first pass transforms x.
+  cudaEvent_t y_ready = nullptr;
+  if (kind == Kind::Ntt && ilog2_ceil(size) > kTileBits) {
+    HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
+    HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
+    HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
+    HG_CUDA(cudaMemcpyAsync(c.Y.p, y, ny * 8, cudaMemcpyHostToDevice, c.copy_stream), "operand upload");
+    HG_CUDA(cudaEventRecord(c.copy_done, c.copy_stream), "operand upload");
+    dx = c.X.u64();
+    dy = c.Y.u64();
+    y_ready = c.copy_done;
+  }
   if (!dx) {
     HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
     HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
@@ -703,7 +744,7 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
     dout = c.OUT.u64();
   }
   switch (kind) {
-    case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st); break;
+    case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st, y_ready); break;
     case Kind::Square: rc = ntt_product_device(dx, nx, nullptr, 0, dout, nd, st); break;
     case Kind::Schoolboy: rc = small_product_device(dx, nx, dy, ny, 0, dout, nd, st); break;
     case Kind::Digit: rc = small_product_device(dx, nx, nullptr, 0, d, dout, nd, st); break;
@@ -1117,8 +1158,12 @@ int hg_shutdown(void) {
   c.tables.release();
   if (c.stream) cudaStreamDestroy(c.stream);
   if (c.ws_done) cudaEventDestroy(c.ws_done);
+  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+  if (c.copy_done) cudaEventDestroy(c.copy_done);
   c.stream = nullptr;
   c.ws_done = nullptr;
+  c.copy_stream = nullptr;
+  c.copy_done = nullptr;
   c.ws_pending = false;
   c.ready = false;
   return HG_OK;
