@@ -353,6 +353,50 @@ double pass_bytes(const PassArgs &a, int readers, int writers) {
   return bytes;
 }
 
+// ---- inter-pass twiddle tables --------------------------------------------
+//
+// A strided pass over blocks of M = R * S residues multiplies row r of column
+// s by w_M^(+-s * bitrev r).  For M up to 2^25 those M twiddles per prime are
+// built once per (M, R, direction) and read by the pass (8 bytes per residue,
+// shared by both operands), which saves the kernel the recurrence that forms
+// them (one Montgomery product per residue).  Larger passes form them.
+constexpr int kPassTwiddleMaxLogM = 25;
+std::mutex g_ptw_mu;
+std::map<std::tuple<int, int, bool>, DevBuf> g_ptw;
+
+const uint64_t *pass_twiddles(int logM, int logR, bool inverse) {
+  if (logM > kPassTwiddleMaxLogM) return nullptr;
+  std::lock_guard<std::mutex> lk(g_ptw_mu);
+  const auto key = std::make_tuple(logM, logR, inverse);
+  auto it = g_ptw.find(key);
+  if (it != g_ptw.end()) return it->second.u64();
+  DevBuf b;
+  const size_t bytes = (static_cast<size_t>(kPrimes) << logM) * sizeof(uint64_t);
+  if (b.ensure(bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;  // no room: the pass forms its twiddles
+  }
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    if (st) cudaStreamDestroy(st);
+    cudaGetLastError();
+    b.release();
+    return nullptr;
+  }
+  cudaStreamDestroy(st);
+  const uint64_t *p = b.u64();
+  g_ptw.emplace(key, b);
+  return p;
+}
+
+void release_pass_twiddles() {
+  std::lock_guard<std::mutex> lk(g_ptw_mu);
+  for (auto &kv : g_ptw) kv.second.release();
+  g_ptw.clear();
+}
+
 // Strided passes [s0, s1) of `plan` (whose last entry is the contiguous
 // pass), forward in order or inverse in reverse order.
 cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, int s0, int s1,
@@ -364,6 +408,7 @@ cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, boo
     a.logS = pp.logS;
     a.logT = pp.logT;
     a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
+    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse);
     cudaError_t e;
     {
       ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, pass_bytes(a, a.nops, a.nops));
@@ -1156,6 +1201,7 @@ int hg_shutdown(void) {
   c.flags.release();
   c.misc.release();
   c.tables.release();
+  release_pass_twiddles();
   if (c.stream) cudaStreamDestroy(c.stream);
   if (c.ws_done) cudaEventDestroy(c.ws_done);
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);

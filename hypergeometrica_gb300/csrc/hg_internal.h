@@ -52,6 +52,10 @@ struct PassArgs {
   uint64_t tiles;              // tiles per (product, operand, prime)
   PrimeConst pc[kPrimes];
   NttTables tb[kPrimes];
+  // Strided passes: the inter-pass twiddles w_M^(+-s * bitrev r) of this
+  // (M, R, direction), Montgomery form, [prime][r][s] with M words per prime
+  // (all primes of the scheme), or null to form them from tb.
+  const uint64_t *ptw;
 };
 
 // Limbs a pass reads for (product, operand), or nullptr when it reads residues.
@@ -106,6 +110,11 @@ cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_
 cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,
                                const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
 cudaError_t launch_scale(uint64_t *a, uint64_t n, uint64_t mont_factor, PrimeConst pc, cudaStream_t st);
+
+// Fill out[j * M + r * S + s] = w_M^(+-s * bitrev_R(r)) (Montgomery form) for
+// the primes j = 0 .. nprimes - 1 of tb, M = 2^logM, R = 2^logR, S = M / R.
+cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse, const NttTables *tb,
+                                 const PrimeConst *pc, int nprimes, cudaStream_t st);
 
 // Tiles a carry-scan launch over n positions uses.
 uint64_t carry_tiles(uint64_t n);

@@ -127,12 +127,16 @@ __device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *d
   for (int i = 0; i < 16; ++i) data[base + (xt | (static_cast<uint32_t>(i) << A))] = v[i];
 }
 
+// Two CTAs of 256 threads per SM (128 registers).  Measured on the 4096-point
+// multiply block: three CTAs at 80 registers, or 768-thread CTAs sharing one
+// twiddle table, run slower than this (register spills, less ILP).
 template <int T, int MODE>
 __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassArgs P) {
   using Gr = Groups<T>;
   constexpr int ATOP = Gr::template A<Gr::G - 1>();
   constexpr int A0 = Gr::template A<0>();
   constexpr int LT = T - 4;                  // log2 threads per block
+  constexpr int NT = kTileThreads;
   constexpr int BPC = 1 << (kTileBits - T);  // blocks per CTA: every CTA has 256 threads
   extern __shared__ uint64_t smem[];
   const uint32_t tid = threadIdx.x;
@@ -155,8 +159,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
   uint64_t *smB = smem + ((BPC + lb) << T);
   // One table of (twiddle, companion) pairs: the forward one, replaced by
   // the inverse one after the pointwise product.
-  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) << kTileBits));
-  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, kTileThreads);
+  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) * BPC << T));
+  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, NT);
   uint64_t nl0 = 0, nl1 = 0;
   const uint64_t *limbs0 = pass_limbs(P, prod, 0, nl0);
   const uint64_t *limbs1 = TWO ? pass_limbs(P, prod, 1, nl1) : nullptr;
@@ -171,36 +175,45 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
     inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
-  } else {
+  } else if constexpr (MODE == kFwd) {
     xt = thread_base<ATOP>(lt);
     if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
     else zero16(v);
     __syncthreads();
     forward_rounds<T>(v, smA, tw, xt, lt, p, c);
-    if constexpr (MODE == kFwd) {
-      if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
-      return;
-    } else {
-      if constexpr (MODE == kMul) {
-        // Park operand 0's spectrum in smA (each thread rereads only its own
-        // words), transform operand 1 through smB.
-        __syncthreads();
-        to_smem<A0>(smA, v, xt);
-        uint32_t xb = thread_base<ATOP>(lt);
-        if (valid) load_block<ATOP>(v, P.data[1] + poff, limbs1, nl1, base, xb, p);
+    if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
+    return;
+  } else {
+    {
+      // The operands' forward transforms share one copy of the round code (a
+      // loop, not unrolled): operand 0's spectrum is parked in smA (each
+      // thread rereads only its own words), operand 1 transforms through smB.
+      constexpr int nop = TWO ? 2 : 1;
+#pragma unroll 1
+      for (int op = 0; op < nop; ++op) {
+        xt = thread_base<ATOP>(lt);
+        if (valid) load_block<ATOP>(v, P.data[op] + poff, op ? limbs1 : limbs0, op ? nl1 : nl0, base, xt, p);
         else zero16(v);
-        forward_rounds<T>(v, smB, tw, xb, lt, p, c);
-        const uint32_t sx = swz(xb);
+        if (op == 0) __syncthreads();  // twiddle table ready
+        forward_rounds<T>(v, op ? smB : smA, tw, xt, lt, p, c);
+        if (TWO && op == 0) {
+          __syncthreads();
+          to_smem<A0>(smA, v, xt);
+        }
+      }
+    }
+    {
+      if constexpr (MODE == kMul) {
+        const uint32_t sx = swz(xt);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(smA[sx ^ swz(static_cast<uint32_t>(i) << A0)], v[i], p, c);
-        xt = xb;
       } else {
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
       __syncthreads();  // every thread is done with the forward table
-      load_sub_twiddles(tw, tb.sub_inv, T, tid, kTileThreads);
+      load_sub_twiddles(tw, tb.sub_inv, T, tid, NT);
       __syncthreads();
       inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
       if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
@@ -266,9 +279,14 @@ __global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, ui
 }
 
 template <int T, int MODE>
-cudaError_t launch_tm(const PassArgs &a, dim3 grid, cudaStream_t st) {
+cudaError_t launch_tm(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
+  constexpr uint64_t bpc = uint64_t(1) << (kTileBits - T);
   constexpr size_t bytes =
-      ((MODE == kMul ? 2u : 1u) << kTileBits) * sizeof(uint64_t) + (1u << (T - 1)) * sizeof(ulonglong2);
+      static_cast<size_t>(MODE == kMul ? 2 : 1) * (1u << kTileBits) * sizeof(uint64_t) +
+      (1u << (T - 1)) * sizeof(ulonglong2);
+  const uint64_t gx = (nblk + bpc - 1) / bpc;
+  if (gx == 0 || gx > 0x7fffffffull) return cudaErrorInvalidValue;
+  const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(a.nprimes));
   // Raise the dynamic shared-memory limit once per instantiation (not on
   // every launch, so that launches can be captured in a CUDA graph).
   static bool raised = false;
@@ -284,20 +302,16 @@ cudaError_t launch_tm(const PassArgs &a, dim3 grid, cudaStream_t st) {
 
 template <int MODE>
 cudaError_t launch_mode(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
-  const uint64_t bpc = 1ull << (kTileBits - a.logT);
-  const uint64_t gx = (nblk + bpc - 1) / bpc;
-  if (gx == 0 || gx > 0x7fffffffull) return cudaErrorInvalidValue;
-  const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(a.nprimes));
   switch (a.logT) {
-    case 4: return launch_tm<4, MODE>(a, grid, st);
-    case 5: return launch_tm<5, MODE>(a, grid, st);
-    case 6: return launch_tm<6, MODE>(a, grid, st);
-    case 7: return launch_tm<7, MODE>(a, grid, st);
-    case 8: return launch_tm<8, MODE>(a, grid, st);
-    case 9: return launch_tm<9, MODE>(a, grid, st);
-    case 10: return launch_tm<10, MODE>(a, grid, st);
-    case 11: return launch_tm<11, MODE>(a, grid, st);
-    case 12: return launch_tm<12, MODE>(a, grid, st);
+    case 4: return launch_tm<4, MODE>(a, nblk, st);
+    case 5: return launch_tm<5, MODE>(a, nblk, st);
+    case 6: return launch_tm<6, MODE>(a, nblk, st);
+    case 7: return launch_tm<7, MODE>(a, nblk, st);
+    case 8: return launch_tm<8, MODE>(a, nblk, st);
+    case 9: return launch_tm<9, MODE>(a, nblk, st);
+    case 10: return launch_tm<10, MODE>(a, nblk, st);
+    case 11: return launch_tm<11, MODE>(a, nblk, st);
+    case 12: return launch_tm<12, MODE>(a, nblk, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -17,6 +17,8 @@
 // once through shared memory, runs the stages of the low four row bits, and
 // applies the inter-pass twiddle to its 16 rows of one column as a geometric
 // sequence beta * gamma^k before storing from registers.
+#include <algorithm>
+
 #include "hg_ntt_rounds.cuh"
 
 namespace hg {
@@ -65,13 +67,24 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
     off0 = base + (static_cast<uint64_t>(xt >> ROWOFF) << logS) + (xt & ((1u << LOGTC) - 1u));
     step = 1ull << (logS + (a - ROWOFF));
   };
-  // The twiddle base and ratio for the thread's column in layout A0.
-  auto twiddles = [&](uint32_t xt, const uint64_t *hi, const uint64_t *lo, uint64_t &beta, uint64_t &gamma) {
+  // The inter-pass twiddles of the thread's 16 rows r = rhi * 16 + i of one
+  // column s (layout A0): from the pass table when there is one, else as the
+  // geometric sequence beta * gamma^bitrev4(i) from the two-level tables.
+  auto inter_pass = [&](uint64_t (&v)[16], uint32_t xt, const uint64_t *hi, const uint64_t *lo) {
     const uint64_t s = s0 + (xt & ((1u << LOGTC) - 1u));
+    const uint32_t rhi = (xt >> (ROWOFF + 4)) & ((1u << (LOGR - 4)) - 1u);
+    if (P.ptw) {
+      const uint64_t *t = P.ptw + (static_cast<uint64_t>(prime) << logM) +
+                          (static_cast<uint64_t>(rhi) << (4 + logS)) + s;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(t + (static_cast<uint64_t>(i) << logS)), p, c);
+      return;
+    }
     uint32_t rrev = 0;
-    if constexpr (LOGR > 4) rrev = bitrev((xt >> (ROWOFF + 4)) & ((1u << (LOGR - 4)) - 1u), LOGR - 4);
-    beta = table_twiddle(s * rrev, logM, hi, lo, p, c);
-    gamma = table_twiddle(s << (LOGR - 4), logM, hi, lo, p, c);
+    if constexpr (LOGR > 4) rrev = bitrev(rhi, LOGR - 4);
+    const uint64_t beta = table_twiddle(s * rrev, logM, hi, lo, p, c);
+    const uint64_t gamma = table_twiddle(s << (LOGR - 4), logM, hi, lo, p, c);
+    geometric_twiddle(v, beta, gamma, p, c);
   };
 
   uint64_t v[16];
@@ -101,9 +114,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
       from_smem<A0>(v, sm, xt);
     }
     stages<4, 0, A0, ROWOFF, 0, LOGR, false, true>(v, tw, xt, p, c);
-    uint64_t beta, gamma;
-    twiddles(xt, tb.hi_fwd, tb.lo_fwd, beta, gamma);
-    geometric_twiddle(v, beta, gamma, p, c);
+    inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
     offsets(xt, A0, off, step);
 #pragma unroll
     for (int i = 0; i < 16; ++i) data[off + i * step] = v[i];
@@ -113,9 +124,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
     offsets(xt, A0, off, step);
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
-    uint64_t beta, gamma;
-    twiddles(xt, tb.hi_inv, tb.lo_inv, beta, gamma);
-    geometric_twiddle(v, beta, gamma, p, c);
+    inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
     __syncthreads();  // twiddle table ready
     stages<4, 0, A0, ROWOFF, 0, LOGR, true, true>(v, tw, xt, p, c);
     if constexpr (G == 2) {
@@ -131,6 +140,22 @@ __global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const Pass
   }
 }
 
+__global__ void pass_twiddles_kernel(uint64_t *out, int logM, int logR, bool inverse, NttTables t0, NttTables t1,
+                                     NttTables t2, PrimeConst c0, PrimeConst c1, PrimeConst c2) {
+  const uint64_t M = uint64_t(1) << logM;
+  const int j = static_cast<int>(blockIdx.y);
+  const NttTables &t = j == 0 ? t0 : (j == 1 ? t1 : t2);
+  const PrimeConst &pc = j == 0 ? c0 : (j == 1 ? c1 : c2);
+  const int logS = logM - logR;
+  for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < M;
+       e += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t r = e >> logS, s = e & ((uint64_t(1) << logS) - 1);
+    const uint64_t E = (s * bitrev(static_cast<uint32_t>(r), logR)) & (M - 1);
+    out[static_cast<uint64_t>(j) * M + e] =
+        table_twiddle(E, logM, inverse ? t.hi_inv : t.hi_fwd, inverse ? t.lo_inv : t.lo_fwd, pc.p, pc.c);
+  }
+}
+
 template <int LOGR>
 cudaError_t launch_r(const PassArgs &a, bool inverse, unsigned grid, cudaStream_t st) {
   if (inverse)
@@ -141,6 +166,18 @@ cudaError_t launch_r(const PassArgs &a, bool inverse, unsigned grid, cudaStream_
 }
 
 }  // namespace
+
+cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse, const NttTables *tb,
+                                 const PrimeConst *pc, int nprimes, cudaStream_t st) {
+  if (nprimes < 1 || nprimes > kPrimes || logR < 1 || logR > 8 || logM <= logR || logM > kLogNmax)
+    return cudaErrorInvalidValue;
+  const uint64_t M = uint64_t(1) << logM;
+  const unsigned gx = static_cast<unsigned>(std::min<uint64_t>((M + 255) / 256, 152 * 64));
+  pass_twiddles_kernel<<<dim3(gx, static_cast<unsigned>(nprimes)), 256, 0, st>>>(
+      out, logM, logR, inverse, tb[0], tb[nprimes > 1 ? 1 : 0], tb[nprimes > 2 ? 2 : 0], pc[0],
+      pc[nprimes > 1 ? 1 : 0], pc[nprimes > 2 ? 2 : 0]);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ntt_strided(const PassArgs &a, bool inverse, cudaStream_t st) {
   const uint64_t grid = a.tiles * a.nprod * static_cast<uint64_t>(a.nops) * static_cast<uint64_t>(a.nprimes);
