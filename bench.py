@@ -17,6 +17,13 @@ second, (na + nb) / seconds per product, summed over ranks.
   cpu_baseline  the oracle (a C restatement of the reference's algorithm,
           per-modulus threads like its with-parallel-work) timed on this
           host on one full product.
+  sweep   a*b and a^2 at 2^18 .. 2^26 limbs per operand.
+  batched 4096 uneven pairs (log-uniform 2^6 .. 2^14 limbs): an autotuned
+          batch replayed from a CUDA graph against one call per product.
+  expt    9^(9^9) with device-resident powers.
+  mpd_pi  Chudnovsky pi/10 through the device-resident multiply service at
+          2^22, 2^24, 2^26 bits, and the reference-exact mpd-pi at 10^4 bits
+          against the CPU oracle.
 
 `--impl reference` times that CPU restatement instead (the reference itself
 is Common Lisp and cannot run here).  With --gpus N under torchrun each rank
@@ -308,6 +315,53 @@ def run_batched(stream, steps: int) -> dict:
     }
 
 
+SWEEP_LOG_SIZES = (18, 20, 22, 24, 26)
+
+
+def run_sweep(stream, peak_gbs: float) -> dict:
+    """The balanced single-product sweep: a x b and a^2 with |a| = |b| = 2^18 ..
+    2^26 limbs (uniform limbs, seeds 11, 12), device-resident, CUDA events.
+    Each line: ms per product, output limbs/s, and the minimum-pass HBM
+    bytes (16 (na + nb) + 192 N for a product, 24 n + 96 N for a square) over
+    the time as a fraction of the measured copy bandwidth."""
+    import numpy as np
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import workloads as W
+
+    out = {"workload": "a*b and a^2, |a| = |b| = 2^k limbs, uniform", "unit": "limbs/s", "lines": []}
+    for k in SWEEP_LOG_SIZES:
+        n = 1 << k
+        a = torch.from_numpy(W.limbs(11, n).view(np.int64)).cuda()
+        b = torch.from_numpy(W.limbs(12, n).view(np.int64)).cuda()
+        o = torch.empty(2 * n, dtype=torch.int64, device="cuda")
+        N = 1 << (k + 1)
+        reps = max(2, min(20, (1 << 26) // n))
+        for kind in ("mul", "sqr"):
+            f = (lambda: D.mul(a, b, o, stream=stream)) if kind == "mul" else (lambda: D.sqr(a, o, stream=stream))
+            for _ in range(2):
+                f()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(reps):
+                f()
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1) / reps
+            D.sync(stream)
+            x = W.limbs(11, n)
+            ok = _residue_ok(o.cpu().numpy().view(np.uint64), x, x if kind == "sqr" else W.limbs(12, n))
+            algo = (16 * 2 * n + 192 * N) if kind == "mul" else (24 * n + 96 * N)
+            out["lines"].append({"log_size": k, "kind": kind, "ms": ms, "limbs_per_s": 2 * n / (ms / 1000.0),
+                                 "hbm_frac": algo / (ms / 1000.0) / 1e9 / peak_gbs, "correct": ok})
+        del a, b, o
+        torch.cuda.empty_cache()
+    out["correct"] = all(line["correct"] for line in out["lines"])
+    return out
+
+
 MPD_BITS = (1 << 22, 1 << 24, 1 << 26)
 MPD_EXACT_BITS = 10000
 
@@ -515,6 +569,9 @@ def run_ours(args) -> None:
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"],
                    "samples": clocks["samples"]},
     }
+    if not args.no_sweep and ws == 1:
+        line["sweep"] = run_sweep(stream, peak)
+        line["correct"] = line["correct"] and line["sweep"]["correct"]
     if not args.no_batched:
         line["batched"] = run_batched(stream, args.steps)
         line["correct"] = line["correct"] and line["batched"]["correct"]
@@ -548,6 +605,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 4096-pair batched-products measurement")
     ap.add_argument("--no-mpd", action="store_true", help="skip the mpd-pi measurement")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 2^18..2^26 balanced-product sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
