@@ -169,6 +169,50 @@ __global__ void __launch_bounds__(kSumThreads) trim_kernel(const VecDesc *descs,
   if (threadIdx.x == 0) sizes[blockIdx.x] = static_cast<uint64_t>(t + 1);
 }
 
+// %multiply-storage/schoolboy (src/mpz-ram.lisp:404-431) for many small
+// products, one thread each: column k of the product is the 192-bit sum of
+// x_i y_(k-i) plus the carry from column k - 1 (< 2^71 for <= 64-limb
+// operands).
+__global__ void small_mul_kernel(const ProductDesc *descs, uint64_t n) {
+  const uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  const ProductDesc d = descs[k];
+  const uint64_t *x = d.x, *y = d.y ? d.y : d.x;
+  uint64_t nx = d.nx, ny = d.y ? d.ny : d.nx;
+  if (nx < ny) {
+    const uint64_t *t = x;
+    x = y;
+    y = t;
+    const uint64_t u = nx;
+    nx = ny;
+    ny = u;
+  }
+  uint64_t w = 0;
+  if (ny > 0) {
+    uint64_t c0 = 0, c1 = 0;
+    for (uint64_t col = 0; col + 1 < nx + ny; ++col) {
+      uint64_t a0 = c0, a1 = c1, a2 = 0;
+      const uint64_t ilo = col >= ny ? col - ny + 1 : 0, ihi = col < nx ? col : nx - 1;
+      for (uint64_t i = ilo; i <= ihi; ++i) {
+        const uint64_t u = x[i], v = y[col - i];
+        const uint64_t lo = u * v, hi = __umul64hi(u, v);
+        a0 += lo;
+        const uint64_t cl = a0 < lo ? 1 : 0;
+        const uint64_t t = a1 + hi;
+        const uint64_t ch = t < hi ? 1 : 0;
+        a1 = t + cl;
+        a2 += ch + (a1 < cl ? 1 : 0);
+      }
+      d.out[col] = a0;
+      c0 = a1;
+      c1 = a2;
+    }
+    d.out[nx + ny - 1] = c0;
+    w = nx + ny;
+  }
+  for (uint64_t i = w; i < d.nout; ++i) d.out[i] = 0;
+}
+
 template <class Desc, class Launch>
 int run_batch(const Desc *host, size_t n, cudaStream_t st, const char *what, Launch launch) {
   if (n == 0) return HG_OK;
@@ -210,6 +254,28 @@ int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *str
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   return run_batch(d.data(), n, st, "signed sums", [&](const SumDesc *dev, unsigned grid) {
     sum_kernel<<<grid, kSumThreads, 0, st>>>(dev, result);
+  });
+}
+
+int hg_mul_small_batch_device(const hg_product *prods, size_t n, void *stream) {
+  if (n && !prods) return lib_fail(HG_ERR_ARG, "null pointer");
+  if (!lib_ready()) return lib_fail(HG_ERR_NOT_INIT, "hg_mul_small_batch_device: call hg_init first");
+  std::vector<ProductDesc> d(n);
+  for (size_t k = 0; k < n; ++k) {
+    const hg_product &p = prods[k];
+    const bool square = p.y == nullptr;
+    const size_t ny = square ? p.nx : p.ny;
+    if (!p.out || (p.nx && !p.x)) return lib_fail(HG_ERR_ARG, "product %zu: null pointer", k);
+    if (p.nx > HG_SMALL_MAX_LIMBS || ny > HG_SMALL_MAX_LIMBS)
+      return lib_fail(HG_ERR_ARG, "product %zu: %zu x %zu limbs exceeds the %d-limb schoolbook limit", k, p.nx, ny,
+                      HG_SMALL_MAX_LIMBS);
+    if (p.nout < p.nx + ny)
+      return lib_fail(HG_ERR_ARG, "product %zu: nout = %zu cannot hold %zu limbs", k, p.nout, p.nx + ny);
+    d[k] = ProductDesc{p.x, p.y, p.nx, ny, p.out, p.nout};
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return run_batch(d.data(), n, st, "small products", [&](const ProductDesc *dev, unsigned count) {
+    small_mul_kernel<<<(count + 127) / 128, 128, 0, st>>>(dev, count);
   });
 }
 

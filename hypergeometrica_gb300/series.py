@@ -184,6 +184,29 @@ def trim_sizes(vecs) -> np.ndarray:
     return _trim_records(rec)
 
 
+SMALL_MAX_LIMBS = 64  # HG_SMALL_MAX_LIMBS
+
+
+def _multiply_records(rec: np.ndarray, service) -> None:
+    """Run (n, 6) hg_product records: by the one-thread-per-product schoolbook
+    kernel when every operand has at most SMALL_MAX_LIMBS limbs (on the torch
+    stream), else through the service (a callable returning it), waiting for
+    them."""
+    import torch
+
+    if rec.shape[0] == 0:
+        return
+    if int(rec[:, 1].max()) <= SMALL_MAX_LIMBS and int(rec[:, 3].max()) <= SMALL_MAX_LIMBS:
+        rec = np.ascontiguousarray(rec, dtype=np.uint64)
+        st = torch.cuda.current_stream()
+        check(load().hg_mul_small_batch_device(rec.ctypes.data_as(ctypes.c_void_p), rec.shape[0], st.cuda_stream))
+        return
+    torch.cuda.current_stream().synchronize()
+    svc = service()
+    svc.submit_records(rec)
+    svc.wait_all()
+
+
 def _trim_records(rec: np.ndarray) -> np.ndarray:
     import torch
 
@@ -268,16 +291,25 @@ def _footprint_bound(total_limbs: int) -> int:
     return 2 * 3 * n * 8
 
 
-def binary_split(series: Series, lower: int, upper: int, service=None) -> Partial:
-    """binary-split (src/binary-splitting.lisp:123-133) on the GPU."""
+def binary_split(series: Series, lower: int, upper: int, service=None, timings: list | None = None) -> Partial:
+    """binary-split (src/binary-splitting.lisp:123-133) on the GPU.  When
+    `timings` is a list, one (height, nodes, seconds of products, seconds of
+    sums and trims) record per height is appended to it, after a
+    ("tree", nodes, seconds) and a ("leaves", count, seconds) record."""
+    import time
+
     import torch
 
     from . import device as D
 
     if upper <= lower:
         raise ValueError("binary-split needs upper > lower")
+    t_start = time.perf_counter()
     lo, hi, left, right, height = _tree(lower, upper)
     nn = lo.size
+    if timings is not None:
+        timings.append(("tree", int(nn), time.perf_counter() - t_start))
+    t_start = time.perf_counter()
     leaves = np.flatnonzero(left < 0)
     ptr = np.zeros((4, nn), dtype=np.uint64)
     size = np.zeros((4, nn), dtype=np.int64)
@@ -312,15 +344,26 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
     arenas = {0: arena0}
     del arena0
     H = int(height.max())
-    own = None
-    if service is None and H > 0:
-        ws = max(64 << 20, _footprint_bound(2 * leaf_limbs))
-        own = D.Service(workspace_bytes=2 * ws, slots=2)
-        service = own
+    if timings is not None:
+        timings.append(("leaves", int(leaves.size), time.perf_counter() - t_start))
+    own = []
+
+    def get_service():
+        """The caller's service, else one opened on first use, sized for the
+        largest product the tree can form."""
+        if service is not None:
+            return service
+        if not own:
+            ws = max(64 << 20, _footprint_bound(2 * leaf_limbs))
+            own.append(D.Service(workspace_bytes=2 * ws, slots=2))
+        return own[0]
+
     torch.cuda.synchronize()
     try:
+        order = np.argsort(height, kind="stable")
+        bounds = np.searchsorted(height[order], np.arange(H + 2))
         for h in range(1, H + 1):
-            idx = np.flatnonzero(height == h)
+            idx = order[bounds[h]: bounds[h + 1]]
             L, R = left[idx], right[idx]
             k = idx.size
             sL, sR = size[:, L], size[:, R]
@@ -346,13 +389,13 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
                 np.concatenate([sR[0], sR[1], sR[2], sL[3], sR[3]]),
                 np.concatenate([aP, aQ, aB, t1, t2]),
                 np.concatenate([szP, szQ, szB, szT1, szT2]))
-            service.submit_records(stage1)
-            service.wait_all()
+            t0 = time.perf_counter()
+            _multiply_records(stage1, get_service)
             stage2 = D.product_records(np.concatenate([pR[2], pL[2]]), np.concatenate([sR[2], sL[2]]),
                                        np.concatenate([t1, t2]), np.concatenate([szT1, szT2]),
                                        np.concatenate([t3, t4]), np.concatenate([szT3, szT4]))
-            service.submit_records(stage2)
-            service.wait_all()
+            _multiply_records(stage2, get_service)
+            t1 = time.perf_counter()
             sgT1, sgT2 = gR[1] * gL[3], gL[0] * gR[3]
             sgT3, sgT4 = gR[2] * sgT1, gL[2] * sgT2
             sums = np.stack([t3, szT3.astype(np.uint64), t4, szT4.astype(np.uint64), aR, szR.astype(np.uint64),
@@ -361,6 +404,8 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
             trims = np.stack([np.concatenate([aP, aQ, aB]),
                               np.concatenate([szP, szQ, szB]).astype(np.uint64)], axis=1)
             tsz = _trim_records(trims)
+            if timings is not None:
+                timings.append((h, int(k), t1 - t0, time.perf_counter() - t1))
             ptr[0, idx], ptr[1, idx], ptr[2, idx], ptr[3, idx] = aP, aQ, aB, aR
             size[0, idx], size[1, idx], size[2, idx] = tsz[:k], tsz[k: 2 * k], tsz[2 * k:]
             size[3, idx] = res[:, 1]
@@ -372,8 +417,8 @@ def binary_split(series: Series, lower: int, upper: int, service=None) -> Partia
             del scratch
             arenas.pop(h - 2, None)
     finally:
-        if own is not None:
-            own.close()
+        for svc in own:
+            svc.close()
 
     def dev_int(j: int) -> DeviceInt:
         if H == 0:

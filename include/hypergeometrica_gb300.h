@@ -198,6 +198,17 @@ typedef struct hg_sum {
  * zero limbs (device int64 array of 2n entries). */
 int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *stream);
 
+/* Largest operand of hg_mul_small_batch_device. */
+#define HG_SMALL_MAX_LIMBS 64
+
+/* %multiply-storage/schoolboy (src/mpz-ram.lisp:404-431) on n small device
+ * products at once (operands of at most HG_SMALL_MAX_LIMBS limbs; y NULL
+ * squares x), one thread per product: out[0, nx + ny) the product, zeros up
+ * to nout.  The mpz-* dispatch sends products with a smaller operand of at
+ * most 100 limbs this way (src/multiply.lisp:37-42); binary splitting's
+ * lowest tree levels consist of them. */
+int hg_mul_small_batch_device(const hg_product *prods, size_t n, void *stream);
+
 typedef struct hg_vec {
     const uint64_t *p; /* device limbs */
     size_t n;

@@ -175,3 +175,40 @@ def test_python_leaves_for_a_series_without_polynomials(hg):
     part = S.binary_split(ser, 0, 90)
     want = O.binary_split((ser.a, ser.b, ser.p, ser.q), 0, 90)
     assert (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int()) == want
+
+
+def test_small_schoolbook_batch(hg):
+    """hg_mul_small_batch_device against Python integers, up to 64 x 64 limbs,
+    squares and zero operands included."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300 import series as S
+
+    rng = np.random.default_rng(17)
+    xs, ys, outs, want = [], [], [], []
+    for k in range(300):
+        nx, ny = int(rng.integers(0, 65)), int(rng.integers(0, 65))
+        a = W.limbs(3 * k + 1, nx)
+        if k % 7 == 2:
+            a = np.full(nx, np.uint64(2**64 - 1))
+        sq = k % 5 == 0
+        b = a if sq else W.limbs(3 * k + 2, ny)
+        ta, _ = _dev(a)
+        tb, _ = _dev(b)
+        nout = a.size + b.size + (k % 3)
+        o = torch.full((max(1, nout),), -1, dtype=torch.int64, device="cuda")
+        xs.append((ta, a.size))
+        ys.append(None if sq else (tb, b.size))
+        outs.append((o, nout))
+        want.append(_as_int(a) * _as_int(b))
+    rec = D.product_records([t.data_ptr() for t, _ in xs], [n for _, n in xs],
+                            [0 if y is None else y[0].data_ptr() for y in ys],
+                            [0 if y is None else y[1] for y in ys],
+                            [o.data_ptr() for o, _ in outs], [n for _, n in outs])
+    torch.cuda.synchronize()
+    S._multiply_records(rec, None)
+    torch.cuda.synchronize()
+    for k, ((o, nout), v) in enumerate(zip(outs, want)):
+        got = o.cpu().numpy().view(np.uint64)[:nout]
+        assert _as_int(got) == v, k
