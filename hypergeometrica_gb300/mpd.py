@@ -176,18 +176,25 @@ def estimate_reciprocal(a: MPD) -> MPD:
 
 
 def mpd_reciprocal(a: MPD, bits: int, service=None, truncate: bool = False) -> MPD:
-    """Newton on f(x) = 1/x - a: x <- x + x h, h = 1 - a x."""
+    """Newton on f(x) = 1/x - a: x <- x + x h, h = 1 - a x.  With truncate,
+    each step works at twice the previous step's precision (a, x and h kept
+    to it), up to the requested digits plus two."""
     digits = max(1, -(-bits // 64))
     x = estimate_reciprocal(a)
     one = integer_mpd(1)
+    prec = 2
     while True:
-        h = mpd_sub(one, mpd_mul(a, x, service))
+        at = mpd_truncate(a, prec + 2) if truncate else a
+        h = mpd_sub(one, mpd_mul(at, x, service))
         zeros, zero = mpd_oom(h)
-        if zero or -zeros >= digits:
+        if (zero or -zeros >= digits) and (not truncate or prec >= digits + 2):
             return x
+        if truncate:
+            h = mpd_truncate(h, prec + 2)
         x = mpd_add(x, mpd_mul(x, h, service))
         if truncate:
-            x = mpd_truncate(x, digits + 2)
+            prec = min(2 * prec, digits + 2)
+            x = mpd_truncate(x, prec + 2)
 
 
 def estimate_inv_sqrt(a: MPD) -> MPD:
@@ -205,18 +212,27 @@ def estimate_inv_sqrt(a: MPD) -> MPD:
 
 
 def mpd_inv_sqrt(a: MPD, bits: int, service=None, truncate: bool = False) -> MPD:
-    """Newton on f(x) = 1/x^2 - a: x <- (2x + x h) / 2, h = 1 - a x^2."""
+    """Newton on f(x) = 1/x^2 - a: x <- (2x + x h) / 2, h = 1 - a x^2.  With
+    truncate, precision doubles step by step as in mpd_reciprocal."""
     digits = max(1, -(-bits // 64))
     x = estimate_inv_sqrt(a)
     one = integer_mpd(1)
+    prec = 2
     while True:
-        h = mpd_sub(one, mpd_mul(a, mpd_mul(x, x, service), service))
+        at = mpd_truncate(a, prec + 2) if truncate else a
+        xx = mpd_mul(x, x, service)
+        if truncate:
+            xx = mpd_truncate(xx, prec + 2)
+        h = mpd_sub(one, mpd_mul(at, xx, service))
         zeros, zero = mpd_oom(h)
-        if zero or -zeros >= digits:
+        if (zero or -zeros >= digits) and (not truncate or prec >= digits + 2):
             return x
+        if truncate:
+            h = mpd_truncate(h, prec + 2)
         x = mpd_half(mpd_add(mpd_add(x, x), mpd_mul(x, h, service)), service)
         if truncate:
-            x = mpd_truncate(x, digits + 2)
+            prec = min(2 * prec, digits + 2)
+            x = mpd_truncate(x, prec + 2)
 
 
 def mpd_sqrt(a: MPD, bits: int, service=None, truncate: bool = False) -> MPD:

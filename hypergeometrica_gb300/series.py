@@ -34,7 +34,7 @@ from typing import Callable
 import numpy as np
 
 from ._lib import check, load
-from .mpz import digits_from_int, int_from_digits
+from .mpz import NTT_MULTIPLY_THRESHOLD, digits_from_int, int_from_digits
 
 
 def one(n: int) -> int:
@@ -152,6 +152,13 @@ def multiply(x: DeviceInt, y: DeviceInt, service=None) -> DeviceInt:
         out.zero_()
         return DeviceInt(1, out, 0)
     xs, ys = x.t[: x.size], (None if square else y.t[: y.size])
+    if not square and min(x.size, y.size) <= NTT_MULTIPLY_THRESHOLD:
+        # mpz-*'s dispatch: a smaller operand of at most 100 limbs goes to the
+        # quadratic method (src/multiply.lisp:37-42), here on the device
+        big, small = (xs, ys) if x.size >= y.size else (ys, xs)
+        D.mul_schoolboy(big, small, out)
+        sizes = trim_sizes([(out, n)])
+        return DeviceInt(x.sign * y.sign, out, int(sizes[0]))
     if service is not None:
         torch.cuda.current_stream().synchronize()
         (t,) = service.submit([(xs, ys, out)])

@@ -67,3 +67,24 @@ def test_truncated_variant_accuracy(hg, bits):
     d = bits * 30103 // 100000
     assert abs(x.digits(d) - O.pi_machin(d - 1)) <= 1 + (10 ** d >> bits)
     assert x.mantissa.size <= -(-(bits + 64) // 64) + 2
+
+
+def test_truncated_variant_2e20_bits_consistent(hg):
+    """At 2^20 bits (too large for an independent pi here): the truncated
+    result agrees with a run at 2^20 + 4096 bits to 2^20 bits, and with the
+    reference-exact 2^16-bit result to 2^16 bits."""
+    from hypergeometrica_gb300 import mpd as G
+
+    bits = 1 << 20
+    a = G.mpd_pi_truncated(bits)
+    b = G.mpd_pi_truncated(bits + 4096)
+    ma, ea = a.to_pair()
+    mb, eb = b.to_pair()
+    # both as floor(2^bits * value)
+    fa = ma >> (-64 * ea - bits) if -64 * ea > bits else ma << (bits + 64 * ea)
+    fb = mb >> (-64 * eb - bits) if -64 * eb > bits else mb << (bits + 64 * eb)
+    assert abs(fa - fb) <= 2
+    x = G.mpd_pi(1 << 16)
+    mx, ex = x.to_pair()
+    fx = mx >> (-64 * ex - (1 << 16))
+    assert abs((fa >> (bits - (1 << 16))) - fx) <= 2
