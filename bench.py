@@ -128,6 +128,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def rank_seeds(rank: int) -> tuple[int, int]:
+    """SplitMix64 seeds of a rank's two operands: each replica multiplies its own."""
+    return 1 + 1000 * rank, 2 + 1000 * rank
+
+
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The slowest rank's time (the job's time); x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(ws: int, units_per_rank_step: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return ws * units_per_rank_step * steps / seconds
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -474,8 +495,9 @@ def run_ours(args) -> None:
 
     H.init(local)
     na = nb = 1 << args.log_size
-    x = W.limbs(1 + 1000 * rank, na)
-    y = W.limbs(2 + 1000 * rank, nb)
+    sx, sy = rank_seeds(rank)
+    x = W.limbs(sx, na)
+    y = W.limbs(sy, nb)
     tx = torch.from_numpy(x.view(np.int64)).cuda()
     ty = torch.from_numpy(y.view(np.int64)).cuda()
     out = torch.empty(na + nb, dtype=torch.int64, device="cuda")
@@ -507,11 +529,7 @@ def run_ours(args) -> None:
         dist.barrier()
     _lib.profile_enable(False)
     prof = _lib.profile_read()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     D.sync(stream)
 
     # End to end through the host entry point, pinned host buffers.
@@ -527,17 +545,13 @@ def run_ours(args) -> None:
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         _lib.check(lib.hg_mul(hx.data_ptr(), na, hy.data_ptr(), nb, hout.data_ptr(), na + nb))
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     clocks = sampler.stop()
     ok = ok and bool(np.array_equal(hout.numpy().view(np.uint64), out.cpu().numpy().view(np.uint64)))
 
     n_out = na + nb
-    value = ws * n_out * args.steps / (ms / 1000.0)
-    e2e_value = ws * n_out * e2e_steps / e2e_s
+    value = job_rate(ws, n_out, args.steps, ms / 1000.0)
+    e2e_value = job_rate(ws, n_out, e2e_steps, e2e_s)
     launches = sum(v["launches"] for v in prof.values())
     dom = max(prof, key=lambda k: prof[k]["ms"])
     peak, peak_kind = _peaks()
