@@ -325,6 +325,32 @@ def run_batched(stream, steps: int) -> dict:
         ms_graph = timed(g.replay, max(3, steps))
     ms_pp = timed(per_product, max(2, min(steps, 5)))
     D.sync(stream)
+
+    # The same pairs through the device-resident service: four client threads
+    # submit 256 pairs at a time; products join batches as slots free up.
+    import threading
+
+    svc_stats, svc_ok = {}, True
+    with D.Service(workspace_bytes=4 << 30, slots=2, max_batch=4096) as svc:
+        svc.submit(items)  # warm
+        svc.wait_all()
+        out_b.fill_(-1)
+        torch.cuda.synchronize()
+        svc.stats(reset=True)
+        chunks = [items[i: i + 256] for i in range(0, len(items), 256)]
+        t0 = time.perf_counter()
+        threads = [threading.Thread(target=lambda c=chunks[k::4]: [svc.submit(x) for x in c]) for k in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        svc.wait_all()
+        wall = time.perf_counter() - t0
+        st = svc.stats()
+        svc_ok = bool(torch.equal(out_b, out_pp))
+        svc_stats = {"products_per_s": BATCH_PAIRS / wall, "wall_ms": 1000 * wall, "p50_us": st["p50_us"],
+                     "p99_us": st["p99_us"], "batches": st["batches"], "slots": st["slots"],
+                     "clients": 4, "chunk": 256, "correct": svc_ok}
     return {
         "metric": "products/s, 4096 uneven pairs", "unit": "products/s",
         "workload": f"{BATCH_PAIRS} pairs, operand sizes log-uniform in [2^6, 2^14] limbs (seeds 41, 42), "
@@ -332,7 +358,7 @@ def run_batched(stream, steps: int) -> dict:
         "graph": BATCH_PAIRS / (ms_graph / 1000.0), "per_product": BATCH_PAIRS / (ms_pp / 1000.0),
         "speedup": ms_pp / ms_graph, "ms_graph": ms_graph, "ms_per_product_path": ms_pp,
         "gpu_launches_graph": launches_batch, "gpu_launches_per_product_path": launches_pp,
-        "autotune_s": tune_s, "correct": correct,
+        "autotune_s": tune_s, "service": svc_stats, "correct": correct and svc_ok,
     }
 
 
