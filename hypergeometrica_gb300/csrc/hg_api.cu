@@ -364,28 +364,36 @@ constexpr int kPassTwiddleMaxLogM = 25;
 std::mutex g_ptw_mu;
 std::map<std::tuple<int, int, bool>, DevBuf> g_ptw;
 
-const uint64_t *pass_twiddles(int logM, int logR, bool inverse) {
+// A table not built yet is not built while `st` is being captured into a
+// CUDA graph (that would allocate and synchronise inside the capture): the
+// pass then forms its twiddles.
+const uint64_t *pass_twiddles(int logM, int logR, bool inverse, cudaStream_t st) {
   if (logM > kPassTwiddleMaxLogM) return nullptr;
   std::lock_guard<std::mutex> lk(g_ptw_mu);
   const auto key = std::make_tuple(logM, logR, inverse);
   auto it = g_ptw.find(key);
   if (it != g_ptw.end()) return it->second.u64();
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return nullptr;
+  }
   DevBuf b;
   const size_t bytes = (static_cast<size_t>(kPrimes) << logM) * sizeof(uint64_t);
   if (b.ensure(bytes) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;  // no room: the pass forms its twiddles
   }
-  cudaStream_t st = nullptr;
-  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
-      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    if (st) cudaStreamDestroy(st);
+  cudaStream_t bs = nullptr;
+  if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess ||
+      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, bs) != cudaSuccess ||
+      cudaStreamSynchronize(bs) != cudaSuccess) {
+    if (bs) cudaStreamDestroy(bs);
     cudaGetLastError();
     b.release();
     return nullptr;
   }
-  cudaStreamDestroy(st);
+  cudaStreamDestroy(bs);
   const uint64_t *p = b.u64();
   g_ptw.emplace(key, b);
   return p;
@@ -408,7 +416,7 @@ cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, boo
     a.logS = pp.logS;
     a.logT = pp.logT;
     a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
-    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse);
+    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse, st);
     cudaError_t e;
     {
       ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, pass_bytes(a, a.nops, a.nops));

@@ -135,3 +135,33 @@ def test_batch_edge_products(hg):
             yv = W.limbs(ny, ny, "uniform")
             want = xi * int.from_bytes(yv.astype("<u8").tobytes(), "little")
         assert int.from_bytes(got.astype("<u8").tobytes(), "little") == want, (nx, ny)
+
+
+def test_graph_capture_before_any_warm_run(hg):
+    """A batch captured into a CUDA graph on its first run, for a transform
+    length (2^16) no earlier test in this file builds inter-pass tables for,
+    replays bit-identically to the single product computed afterwards."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+
+    nx, ny = 5 * 4096 + 17, 3 * 4096 + 5
+    x = _dev(W.limbs(901, nx))
+    y = _dev(W.limbs(902, ny))
+    out = torch.full((nx + ny,), -1, dtype=torch.int64, device="cuda")
+    b = D.Batch([(x, y, out)], autotune=False)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        b.run(s)
+    got = []
+    for _ in range(2):
+        out.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        got.append(out.clone())
+    want = torch.full((nx + ny,), -1, dtype=torch.int64, device="cuda")
+    D.mul(x, y, want)
+    D.sync()
+    assert torch.equal(got[0], want) and torch.equal(got[1], want)
