@@ -405,7 +405,35 @@ def run_sweep(stream, peak_gbs: float) -> dict:
                                  "hbm_frac": algo / (ms / 1000.0) / 1e9 / peak_gbs, "correct": ok})
         del a, b, o
         torch.cuda.empty_cache()
-    out["correct"] = all(line["correct"] for line in out["lines"])
+    # Unbalanced and edge-value products: 2^24 x 2^16, 2^25 x 2^20, 2^20 x 2^6
+    # limbs, uniform, all-ones (the longest carry chains) and 1%-nonzero limbs, through
+    # the NTT product (hg_mul_device, mpz-*/ntt semantics).
+    out["unbalanced"] = []
+    for ka, kb in ((24, 16), (25, 20), (20, 6)):
+        na, nb = 1 << ka, 1 << kb
+        for dist in ("uniform", "ones", "sparse"):
+            xh, yh = W.limbs(13, na, dist), W.limbs(14, nb, dist)
+            a = torch.from_numpy(xh.view(np.int64)).cuda()
+            b = torch.from_numpy(yh.view(np.int64)).cuda()
+            o = torch.empty(na + nb, dtype=torch.int64, device="cuda")
+            reps = max(2, min(10, (1 << 26) // na))
+            for _ in range(2):
+                D.mul(a, b, o, stream=stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(reps):
+                D.mul(a, b, o, stream=stream)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1) / reps
+            D.sync(stream)
+            ok = _residue_ok(o.cpu().numpy().view(np.uint64), xh, yh)
+            out["unbalanced"].append({"log_sizes": [ka, kb], "dist": dist, "ms": ms,
+                                      "limbs_per_s": (na + nb) / (ms / 1000.0), "correct": ok})
+            del a, b, o
+        torch.cuda.empty_cache()
+    out["correct"] = all(line["correct"] for line in out["lines"] + out["unbalanced"])
     return out
 
 
