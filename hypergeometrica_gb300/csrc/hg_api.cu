@@ -1329,6 +1329,14 @@ int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, siz
   return small_product_device(x, nx, y, ny, 0, out, nout, static_cast<cudaStream_t>(stream));
 }
 
+int hg_butterfly_peak(double *butterflies_per_s) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!butterflies_per_s) return fail(HG_ERR_ARG, "null pointer");
+  return butterfly_peak(butterflies_per_s, g_ctx.pc[0], g_ctx.tb[0].sub_fwd);
+}
+
 int hg_sync(void *stream) {
   std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
   int rc = ensure_init();

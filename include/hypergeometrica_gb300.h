@@ -142,6 +142,12 @@ int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, siz
 int hg_mul_device_noalloc(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
                           void *stream);
 
+/* No counterpart in the reference (measurement): the rate, in radix-2
+ * butterflies per second, of a memory-free network of the library's modular
+ * butterflies (half forward DIF, half inverse DIT) over every SM: the
+ * integer-pipe ceiling the NTT passes are measured against. */
+int hg_butterfly_peak(double *butterflies_per_s);
+
 /* Wait for the library's work on stream (NULL = all of it) and report any
  * error latched on the device since the last hg_sync. */
 int hg_sync(void *stream);
