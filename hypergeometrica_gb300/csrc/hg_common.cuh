@@ -94,11 +94,6 @@ __device__ __forceinline__ uint64_t shoup_mul(uint64_t a, uint64_t w, uint64_t w
   return r >= p ? r - p : r;
 }
 
-// A twiddle with its Shoup companion.
-struct Tw {
-  uint64_t w, wq;
-};
-
 // x mod p for any 64-bit x (x < 4p because p > 2^62).
 __device__ __forceinline__ uint64_t reduce64(uint64_t x, uint64_t p) {
   const uint64_t p2 = p << 1;
