@@ -26,8 +26,11 @@ namespace {
 
 using namespace rounds;
 
+// Four CTAs of 256 threads per SM (64 registers, a few spilled words): on
+// the 2^25-point passes faster than three (80 registers), two (128) or five
+// (48).
 template <int LOGR, bool INV>
-__global__ void __launch_bounds__(kTileThreads, 3) ntt_strided_kernel(const PassArgs P) {
+__global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const PassArgs P) {
   constexpr int T = kTileBits;
   constexpr int LOGTC = T - LOGR;  // log2 columns per tile
   constexpr int ROWOFF = LOGTC;    // tile bit of row bit 0
