@@ -17,7 +17,18 @@ struct NttTables {
   const uint64_t *lo_fwd;     // w_{2^30}^e,          e < 2^15, Montgomery form
   const uint64_t *hi_inv;
   const uint64_t *lo_inv;
+  // Sub-transform tables of every block size R = 2^T, T = 1..12, in the
+  // contiguous pass's swizzled order: entry swz_tw(e) of the table of T is
+  // (w_R^e, companion), e < R / 2.  The forward table of T starts at entry
+  // 2^(T-1) - 1, its inverse kSwzInverse entries later.
+  const ulonglong2 *swz;
 };
+
+constexpr uint32_t kSwzInverse = (1u << kTileBits) - 1;  // entries in all forward tables
+
+__host__ __device__ __forceinline__ const ulonglong2 *swz_table(const NttTables &t, int T, bool inverse) {
+  return t.swz + (inverse ? kSwzInverse : 0u) + (1u << (T - 1)) - 1u;
+}
 
 // One product of a batch, as the kernels read it.  y == nullptr squares x.
 struct ProductDesc {

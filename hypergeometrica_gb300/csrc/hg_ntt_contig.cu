@@ -127,11 +127,12 @@ __device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *d
   for (int i = 0; i < 16; ++i) data[base + (xt | (static_cast<uint32_t>(i) << A))] = v[i];
 }
 
-// Two CTAs of 256 threads per SM (128 registers).  Measured on the 4096-point
-// multiply block: three CTAs at 80 registers, or 768-thread CTAs sharing one
-// twiddle table, run slower than this (register spills, less ILP).
+// CTAs of 256 threads per SM: three (80 registers) where the rounds fit
+// without spilling, two (128 registers) for the 9..11-bit blocks.
+__host__ __device__ constexpr int contig_min_blocks(int T) { return (T >= 9 && T <= 11) ? 2 : 3; }
+
 template <int T, int MODE>
-__global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassArgs P) {
+__global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig_kernel(const PassArgs P) {
   using Gr = Groups<T>;
   constexpr int ATOP = Gr::template A<Gr::G - 1>();
   constexpr int A0 = Gr::template A<0>();
@@ -157,10 +158,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
   constexpr bool TWO = (MODE == kMul);
   uint64_t *smA = smem + (lb << T);
   uint64_t *smB = smem + ((BPC + lb) << T);
-  // One table of (twiddle, companion) pairs: the forward one, replaced by
-  // the inverse one after the pointwise product.
-  ulonglong2 *tw = reinterpret_cast<ulonglong2 *>(smem + ((TWO ? 2u : 1u) * BPC << T));
-  load_sub_twiddles(tw, MODE == kInv ? tb.sub_inv : tb.sub_fwd, T, tid, NT);
+  // The (twiddle, companion) pairs of the 2^T-point sub-transform, read from
+  // the swizzled device tables (small, and shared by every CTA: they stay in
+  // L1), forward first, inverse after the pointwise product.
+  const ulonglong2 *tw = swz_table(tb, T, MODE == kInv);
   uint64_t nl0 = 0, nl1 = 0;
   const uint64_t *limbs0 = pass_limbs(P, prod, 0, nl0);
   const uint64_t *limbs1 = TWO ? pass_limbs(P, prod, 1, nl1) : nullptr;
@@ -171,7 +172,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
     xt = thread_base<A0>(lt);
     if (valid) load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
     else zero16(v);
-    __syncthreads();
     inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
@@ -179,7 +179,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
     xt = thread_base<ATOP>(lt);
     if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
     else zero16(v);
-    __syncthreads();
     forward_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
     return;
@@ -194,7 +193,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
         xt = thread_base<ATOP>(lt);
         if (valid) load_block<ATOP>(v, P.data[op] + poff, op ? limbs1 : limbs0, op ? nl1 : nl0, base, xt, p);
         else zero16(v);
-        if (op == 0) __syncthreads();  // twiddle table ready
         forward_rounds<T>(v, op ? smB : smA, tw, xt, lt, p, c);
         if (TWO && op == 0) {
           __syncthreads();
@@ -212,10 +210,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) ntt_contig_kernel(const PassA
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
-      __syncthreads();  // every thread is done with the forward table
-      load_sub_twiddles(tw, tb.sub_inv, T, tid, NT);
-      __syncthreads();
-      inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
+      inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
       if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     }
   }
@@ -281,9 +276,7 @@ __global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, ui
 template <int T, int MODE>
 cudaError_t launch_tm(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
   constexpr uint64_t bpc = uint64_t(1) << (kTileBits - T);
-  constexpr size_t bytes =
-      static_cast<size_t>(MODE == kMul ? 2 : 1) * (1u << kTileBits) * sizeof(uint64_t) +
-      (1u << (T - 1)) * sizeof(ulonglong2);
+  constexpr size_t bytes = static_cast<size_t>(MODE == kMul ? 2 : 1) * (1u << kTileBits) * sizeof(uint64_t);
   const uint64_t gx = (nblk + bpc - 1) / bpc;
   if (gx == 0 || gx > 0x7fffffffull) return cudaErrorInvalidValue;
   const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(a.nprimes));
