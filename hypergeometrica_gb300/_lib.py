@@ -82,6 +82,7 @@ SIGNATURES = {
     "hg_last_error": (ctypes.c_int, [ctypes.c_char_p, _sz]),
     "hg_scheme_moduli": (ctypes.c_int, [_u64p, ctypes.c_int]),
     "hg_ntt_length": (_sz, [_sz, _sz]),
+    "hg_chunk_plan": (ctypes.c_int, [_sz, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
     "hg_mul": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
     "hg_sqr": (ctypes.c_int, [_vp, _sz, _vp, _sz]),
     "hg_mul_schoolboy": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
@@ -115,6 +116,17 @@ SIGNATURES = {
     "hg_profile_read": (ctypes.c_int, [_u64p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                        ctypes.c_int]),
 }
+
+def chunk_plan(nx: int, ny: int):
+    """(log2 transform length, chunk limbs, chunks) of an nx x ny product run
+    in chunks, or None when it runs as one transform."""
+    L = ctypes.c_int()
+    c = _sz()
+    k = _sz()
+    if not load().hg_chunk_plan(nx, ny, ctypes.byref(L), ctypes.byref(c), ctypes.byref(k)):
+        return None
+    return L.value, c.value, k.value
+
 
 KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "middle", "carry", "small", "other"]
 

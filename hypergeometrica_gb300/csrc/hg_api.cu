@@ -7,6 +7,7 @@
 // the NTT passes for a transform length and enqueues the kernels of one
 // product: forward passes (the first reads the limbs and reduces them),
 // pointwise product, inverse passes, reconstruction + carry.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -370,7 +371,8 @@ PassArgs base_args(int L, int nops) {
 // Algorithmic bytes of a launch over nops operands: every residue written
 // once, every input read once (limbs when a pass reduces them itself).
 double pass_bytes(const PassArgs &a, int readers, int writers) {
-  const double words = static_cast<double>(a.nprimes) * static_cast<double>(uint64_t(1) << a.logN);
+  const double words =
+      static_cast<double>(a.nprimes) * static_cast<double>(uint64_t(1) << a.logN) * static_cast<double>(a.nprod);
   double bytes = 8.0 * words * writers;
   for (int op = 0; op < readers; ++op)
     bytes += a.limbs[op] ? 8.0 * static_cast<double>(a.nlimbs[op]) : 8.0 * words;
@@ -525,7 +527,133 @@ int check_len(int L) {
   return HG_OK;
 }
 
+// ---- unbalanced products in chunks ----------------------------------------
+//
+// When one operand is much longer than the other, one transform of the whole
+// product (N = pow2 >= nx + ny, src/ntt-multiply.lisp:174-254) spends most of
+// its work on zero padding.  The long operand is cut into K chunks of C limbs
+// instead; the short one (ns limbs) is transformed once to a 2^L-point
+// spectrum, 2^L >= C + ns; each chunk's 2^L-point transform is multiplied by
+// that spectrum and transformed back, all chunks in one launch per pass; the
+// reconstruction adds the two chunk products that meet at each position (the
+// product is the same integer: sum_k chunk_k * short * 2^(64 C k)).
+struct ChunkPlan {
+  int L = 0;
+  uint64_t chunk = 0, nchunks = 0;
+};
+
+// Cost of a transform of 2^L points in units of one radix-2 stage over one
+// point: L stages plus about kPassCost stages' worth of memory passes.  On
+// GB300 the measured time of chunked products is 0.93-0.97 of this model's
+// ratio to one transform (2^16..2^25 long operands, ratios 0.17-0.80).
+constexpr double kPassCost = 4.0;
+// Chunk only when the estimate is below this fraction of one transform.
+constexpr double kChunkGain = 0.95;
+
+// The cheapest chunking of a long operand of nl limbs and a short one of ns
+// <= nl limbs, or false when one transform of the whole product is cheaper.
+// C = (2^L - ns) rounded down to a multiple of 8 (>= 2^(L-1) because
+// 2^L >= 2 pow2(ns) >= 16), so that at most two chunk products meet at any
+// position of the result.
+bool plan_chunks(uint64_t nl, uint64_t ns, ChunkPlan &cp) {
+  if (ns == 0 || nl < ns) return false;
+  const int Lf = ilog2_ceil(nl + ns);
+  const auto cost = [](double transforms, int L) { return transforms * std::ldexp(L + kPassCost, L); };
+  double best = kChunkGain * cost(3.0, Lf);
+  bool found = false;
+  const int Lmin = std::max(4, ilog2_ceil(ns) + 1);
+  for (int L = Lmin; L < Lf && L <= Lmin + 4; ++L) {
+    const uint64_t T = uint64_t(1) << L;
+    const uint64_t c = (T - ns) & ~uint64_t(7);
+    const uint64_t k = (nl + c - 1) / c;
+    if (k < 2) continue;
+    const double e = cost(2.0 * static_cast<double>(k) + 1.0, L);
+    if (e < best) {
+      best = e;
+      cp = ChunkPlan{L, c, k};
+      found = true;
+    }
+  }
+  return found;
+}
+
+// The chunked schedule of ntt_product_device.  Chunk k's residues occupy
+// workspace A at k * 3 * 2^L words, the short operand's spectrum workspace
+// B.  Caller's operand 0 (x) is resident; when y_ready is given, y may still
+// be in flight, so the work on x's role comes first.
+int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,
+                         uint64_t nout, const ChunkPlan &cp, cudaStream_t st, cudaEvent_t y_ready) {
+  Context &c = g_ctx;
+  const bool x_long = nx >= ny;
+  const uint64_t *lng = x_long ? x : y, *sht = x_long ? y : x;
+  const uint64_t nl = x_long ? nx : ny, ns = x_long ? ny : nx;
+  const int L = cp.L;
+  const uint64_t T = uint64_t(1) << L;
+  const uint64_t slab = static_cast<uint64_t>(kPrimes) * T;
+  HG_CUDA(ws_acquire(st), "workspace ordering");
+  if (c.A.bytes < cp.nchunks * slab * 8 || c.B.bytes < slab * 8) {
+    HG_CUDA(cudaDeviceSynchronize(), "sync before workspace growth");
+    HG_CUDA(c.A.ensure(cp.nchunks * slab * 8), "workspace allocation");
+    HG_CUDA(c.B.ensure(slab * 8), "workspace allocation");
+  }
+  const std::vector<PassPlan> plan = plan_passes(L);
+  const bool one_pass = plan.size() == 1;
+  PassArgs a = base_args(L, 1);  // the chunks
+  a.data[0] = c.A.u64();
+  a.data[1] = c.B.u64();
+  a.limbs[0] = lng;
+  a.nlimbs[0] = nl;
+  a.chunk = cp.chunk;
+  a.nprod = cp.nchunks;
+  a.ws_stride = slab;
+  PassArgs sp = base_args(L, 1);  // the short operand's spectrum
+  sp.data[0] = c.B.u64();
+  sp.limbs[0] = sht;
+  sp.nlimbs[0] = ns;
+  auto chunks_forward = [&]() -> int {
+    HG_CUDA(run_strided(a, plan, false, st), "forward transform");
+    return HG_OK;
+  };
+  auto spectrum_forward = [&]() -> int {
+    HG_CUDA(run_strided(sp, plan, false, st), "forward transform");
+    PassArgs f = sp;
+    if (!one_pass) f.limbs[0] = nullptr;
+    HG_CUDA(run_contig(f, plan.back(), kContigFwd, st), "forward transform");
+    return HG_OK;
+  };
+  int rc = x_long ? chunks_forward() : spectrum_forward();
+  if (rc) return rc;
+  if (y_ready) HG_CUDA(cudaStreamWaitEvent(st, y_ready, 0), "operand upload ordering");
+  rc = x_long ? spectrum_forward() : chunks_forward();
+  if (rc) return rc;
+  {
+    PassArgs m = a;
+    if (!one_pass) m.limbs[0] = nullptr;
+    HG_CUDA(run_contig(m, plan.back(), kContigMulSpec, st), "middle pass");
+  }
+  PassArgs inv = base_args(L, 1);
+  inv.data[0] = c.A.u64();
+  inv.nprod = cp.nchunks;
+  inv.ws_stride = slab;
+  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
+  const uint64_t size = nx + ny;
+  if (nout > size) HG_CUDA(cudaMemsetAsync(out + size, 0, (nout - size) * sizeof(uint64_t), st), "zero tail");
+  ScanState ss;
+  rc = scan_state(carry_tiles(size), &ss);
+  if (rc) return rc;
+  uint64_t tiles = 0;
+  {
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(size));
+    HG_CUDA(launch_crt_carry_chunks(c.A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L), out, size, ss, st,
+                                    &tiles),
+            "reconstruction");
+  }
+  HG_CUDA(ws_release(st), "workspace ordering");
+  return HG_OK;
+}
+
 // |x| * |y| (or |x|^2 when y == nullptr) into out[0, nout) on device memory.
+// An unbalanced pair runs in chunks (chunk_product_device).
 // When y_ready is given (two operands), operand 1's limbs may still be in
 // flight: the first strided pass runs for operand 0 alone, then waits for the
 // event and runs for operand 1, so that an upload of y overlaps it.
@@ -542,6 +670,9 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     HG_CUDA(cudaMemsetAsync(out, 0, nout * sizeof(uint64_t), st), "zero product");
     return HG_OK;
   }
+  ChunkPlan cp;
+  if (!square && plan_chunks(std::max(nx, ny), std::min(nx, ny), cp))
+    return chunk_product_device(x, nx, y, ny, out, nout, cp, st, y_ready);
   const int L = ilog2_ceil(size);
   int rc = check_len(L);
   if (rc) return rc;
@@ -1264,6 +1395,16 @@ size_t hg_ntt_length(size_t nx, size_t ny) {
   size_t r = 1;
   while (r < s) r <<= 1;
   return r;
+}
+
+int hg_chunk_plan(size_t nx, size_t ny, int *log_len, size_t *chunk, size_t *nchunks) {
+  if (!log_len || !chunk || !nchunks) return 0;
+  hg::ChunkPlan cp;
+  if (!hg::plan_chunks(std::max(nx, ny), std::min(nx, ny), cp)) return 0;
+  *log_len = cp.L;
+  *chunk = cp.chunk;
+  *nchunks = cp.nchunks;
+  return 1;
 }
 
 int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout) {

@@ -94,6 +94,65 @@ struct CrtProducer {
   }
 };
 
+// The product of a long operand cut into chunks of `chunk` limbs with a
+// short one: chunk k's cyclic product (2^logN > chunk + short - 1 points, no
+// wrap) covers result positions [k chunk, k chunk + 2^logN), and chunk >=
+// 2^(logN-1) makes at most two chunks meet at a position.  Their residues
+// are added before the reconstruction: the sum of the two coefficients is
+// below 2 * short * 2^128, far below p0 p1 p2, so Garner's value of the
+// summed residues is the exact sum.
+struct ChunkProducer {
+  CrtProducer crt;      // res = chunk 0's residues, n = 2^logN
+  uint64_t stride;      // words between consecutive chunks' residues
+  uint64_t chunk, nchunks;
+
+  __device__ __forceinline__ uint64_t sum_res(const uint64_t *r0, const uint64_t *r1, int j) const {
+    const uint64_t p = crt.k.pc[j].p;
+    const uint64_t a = r0 ? r0[j * crt.n] : 0, b = r1 ? r1[j * crt.n] : 0;
+    return add_mod(a, b, p);
+  }
+
+  // Residue pointers of position i: the chunk that starts at or below i, and
+  // the one before it when position i is inside its product.
+  __device__ __forceinline__ void sources(uint64_t i, const uint64_t *&r0, const uint64_t *&r1) const {
+    const uint64_t k = i / chunk, o = i - k * chunk;
+    r0 = k < nchunks ? crt.res + k * stride + o : nullptr;
+    r1 = (k >= 1 && k - 1 < nchunks && o + chunk < crt.n) ? crt.res + (k - 1) * stride + o + chunk : nullptr;
+  }
+
+  __device__ __forceinline__ V3 at(uint64_t, uint64_t i) const {
+    const uint64_t *r0, *r1;
+    sources(i, r0, r1);
+    return crt.garner(sum_res(r0, r1, 0), sum_res(r0, r1, 1), sum_res(r0, r1, 2));
+  }
+
+  // Eight positions from i0 (a multiple of 8, as is chunk): one chunk pair.
+  __device__ __forceinline__ void eight(uint64_t, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+    if (i0 + 8 > nproc) {
+#pragma unroll
+      for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? at(0, i0 + k8) : V3{0, 0, 0};
+      return;
+    }
+    const uint64_t *r0, *r1;
+    sources(i0, r0, r1);
+    uint64_t r[3][8];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const uint64_t p = crt.k.pc[j].p;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ulonglong2 a = make_ulonglong2(0, 0), b = make_ulonglong2(0, 0);
+        if (r0) a = __ldg(reinterpret_cast<const ulonglong2 *>(r0 + j * crt.n) + q);
+        if (r1) b = __ldg(reinterpret_cast<const ulonglong2 *>(r1 + j * crt.n) + q);
+        r[j][2 * q] = add_mod(a.x, b.x, p);
+        r[j][2 * q + 1] = add_mod(a.y, b.y, p);
+      }
+    }
+#pragma unroll
+    for (int k8 = 0; k8 < 8; ++k8) v[k8] = crt.garner(r[0][k8], r[1][k8], r[2][k8]);
+  }
+};
+
 struct ConvProducer {
   const uint64_t *x;
   uint64_t nx;
@@ -364,6 +423,21 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
   CrtProducer prod{res, n, cc};
   carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, nullptr, 0, ss, batch, tpp,
                                                                                    ws_stride, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int logN, uint64_t chunk,
+                                    uint64_t nchunks, const CrtConst &cc, uint64_t *out, uint64_t nproc,
+                                    const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
+  const uint64_t n = 1ull << logN;
+  if (chunk % 8 || 2 * chunk < n || chunk > n || ws_stride % 2) return cudaErrorInvalidValue;
+  const uint64_t tiles = carry_tiles(nproc);
+  *tiles_used = tiles;
+  if (tiles == 0) return cudaSuccess;
+  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  ChunkProducer prod{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks};
+  carry_kernel<ChunkProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                     0, 0, 0);
   return cudaGetLastError();
 }
 

@@ -50,6 +50,8 @@ struct PassArgs {
   const uint64_t *limbs[2];    // single product: this pass reads and reduces limbs
   uint64_t nlimbs[2];
   const ProductDesc *batch;    // batch: operands of product k are batch[k].x / .y
+  uint64_t chunk;              // single product cut into chunks: product k reads
+                               // operand 0's limbs [k * chunk, (k + 1) * chunk)
   int read_limbs;              // batch: this pass reads and reduces limbs
   int nops;                    // operands handled by this launch
   int logN;
@@ -79,6 +81,11 @@ __host__ __device__ __forceinline__ const uint64_t *pass_limbs(const PassArgs &P
     return op ? d.y : d.x;
   }
   nl = P.nlimbs[op];
+  if (P.chunk && op == 0 && P.limbs[0]) {
+    const uint64_t o = prod * P.chunk;
+    nl = nl > o ? (nl - o < P.chunk ? nl - o : P.chunk) : 0;
+    return P.limbs[0] + o;
+  }
   return P.limbs[op];
 }
 
@@ -105,8 +112,10 @@ struct ScanState {
 // Strided pass (hg_ntt_strided.cu): 4 <= logR <= 8, logT = 12.
 cudaError_t launch_ntt_strided(const PassArgs &a, bool inverse, cudaStream_t st);
 // Contiguous pass (hg_ntt_contig.cu), mode: 0 forward, 1 inverse, 2 product
-// of operands 0 and 1, 3 square of operand 0; logR == logT <= 12.
-constexpr int kContigFwd = 0, kContigInv = 1, kContigMul = 2, kContigSqr = 3;
+// of operands 0 and 1, 3 square of operand 0, 4 product of operand 0 with a
+// finished spectrum at data[1] that every product of the launch shares;
+// logR == logT <= 12.
+constexpr int kContigFwd = 0, kContigInv = 1, kContigMul = 2, kContigSqr = 3, kContigMulSpec = 4;
 cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st);
 cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, uint64_t *out, uint64_t nout,
                              const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
@@ -114,6 +123,15 @@ cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, 
 // residues start ws_stride words apart at res.
 cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int logN, const CrtConst &cc,
                                    const ProductDesc *batch, uint64_t nprod, const ScanState &ss, cudaStream_t st);
+// Reconstruction + carry of a product computed in chunks: chunk k's
+// residues ([3][2^logN], unscaled inverse) start k * ws_stride words past
+// res and hold the product of limbs [k * chunk, (k + 1) * chunk) of the long
+// operand with the short one; position i of the result sums chunk i / chunk
+// at i % chunk and the chunk before it at i % chunk + chunk.  Writes
+// out[0, nproc).  Needs 2^(logN-1) <= chunk, chunk a multiple of 8.
+cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int logN, uint64_t chunk,
+                                    uint64_t nchunks, const CrtConst &cc, uint64_t *out, uint64_t nproc,
+                                    const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
 // Zero out[N, nout) of every product (out[0, nout) when N == 0).
 cudaError_t launch_zero_tails(const ProductDesc *batch, uint64_t nprod, uint64_t N, cudaStream_t st);
 cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,

@@ -9,7 +9,10 @@
 //   kMul  both operands' forward stages, the pointwise product
 //         (multiply-pointwise!, src/ntt-multiply.lisp:88-99) and the
 //         inverse stages: the block is read once per operand, written once,
-//   kSqr  the same for one operand squared (src/ntt-multiply.lisp:136-144).
+//   kSqr  the same for one operand squared (src/ntt-multiply.lisp:136-144),
+//   kMulSpec  operand 0's forward stages, the pointwise product with a
+//         finished spectrum that every product of the launch shares, and the
+//         inverse stages (the chunks of an unbalanced product).
 // For transforms of at most 2^12 points this is the whole product's NTT work,
 // and the kernel reads the limbs and reduces them itself.
 //
@@ -24,7 +27,7 @@ namespace {
 
 using namespace rounds;
 
-constexpr int kFwd = 0, kInv = 1, kMul = 2, kSqr = 3;
+constexpr int kFwd = 0, kInv = 1, kMul = 2, kSqr = 3, kMulSpec = 4;
 
 // Register block of row group g in a 2^T block: groups of four row bits from
 // the bottom; the top group may be partial and then shares its register
@@ -182,6 +185,20 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
     forward_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
     return;
+  } else if constexpr (MODE == kMulSpec) {
+    xt = thread_base<ATOP>(lt);
+    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
+    else zero16(v);
+    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
+    // The shared spectrum sits where kFwd stores it, without a product offset.
+    if (valid) {
+      const uint64_t *spec = P.data[1] + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride + base;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(spec + (xt | (static_cast<uint32_t>(i) << A0))), p, c);
+    }
+    inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
+    if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
+    return;
   } else {
     {
       // The operands' forward transforms share one copy of the round code (a
@@ -316,7 +333,7 @@ cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
   if (nblk == 0 || a.logS != 0 || a.logR != a.logT || a.nprimes < 1 || a.nprimes > kPrimes)
     return cudaErrorInvalidValue;
   if (a.logT < 4) {
-    if (a.logT < 1 || a.logT != a.logN || a.tiles != 1 || a.nprod > 0x7fffffffull) return cudaErrorInvalidValue;
+    if (mode == kMulSpec || a.logT < 1 || a.logT != a.logN || a.tiles != 1 || a.nprod > 0x7fffffffull) return cudaErrorInvalidValue;
     ntt_tiny_kernel<<<dim3(static_cast<unsigned>(a.nprod), static_cast<unsigned>(a.nprimes)), 1, 0, st>>>(a, mode);
     return cudaGetLastError();
   }
@@ -325,6 +342,7 @@ cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
     case kInv: return launch_mode<kInv>(a, nblk, st);
     case kMul: return launch_mode<kMul>(a, nblk, st);
     case kSqr: return launch_mode<kSqr>(a, nblk, st);
+    case kMulSpec: return launch_mode<kMulSpec>(a, nblk, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -72,6 +72,15 @@ int hg_scheme_moduli(uint64_t *out, int cap);
 // hg_ntt_length(nx, nx) (:103).
 size_t hg_ntt_length(size_t nx, size_t ny);
 
+// How hg_mul, hg_mul_device and hg_mpz_mul run an unbalanced product (no
+// counterpart in the reference, whose mpz-*/ntt always runs one transform of
+// hg_ntt_length(nx, ny) points).  Returns 1 when the longer operand is cut
+// into *nchunks chunks of *chunk limbs, each multiplied by the shorter one
+// with transforms of 2^*log_len points (the result is the same integer);
+// 0 when the product runs as one transform, or on a null pointer.  Host
+// arithmetic only: needs no device and no hg_init.
+int hg_chunk_plan(size_t nx, size_t ny, int *log_len, size_t *chunk, size_t *nchunks);
+
 /* ---- products on host memory ------------------------------------------ */
 
 // mpz-*/ntt (src/ntt-multiply.lisp:174-254): |x| * |y| through the three-prime

@@ -42,6 +42,31 @@ def test_host_only_queries(lib):
     assert list(buf)[:3] == [0x6280000000000001, 0x5700000000000001, 0x4180000000000001]
 
 
+def test_chunk_plan_invariants(lib):
+    """The unbalanced-product planner: chunks of C limbs (a multiple of 8)
+    against the short operand fit a 2^L-point cyclic product without wrap,
+    at most two chunk products meet at any position, the chunks cover the
+    long operand exactly, and balanced products are not chunked."""
+    from hypergeometrica_gb300 import _lib
+
+    assert _lib.chunk_plan(1 << 24, 1 << 24) is None
+    assert _lib.chunk_plan(100000, 31000) is None
+    assert _lib.chunk_plan(0, 5) is None
+    seen = set()
+    for nl, ns in [(1 << 24, 1 << 16), (1 << 25, 1 << 20), (1 << 20, 1 << 6), (65536, 64), (3000, 7),
+                   (1 << 18, 5), (200003, 1000), ((1 << 20) + 12345, 3001), (1 << 26, 2), (10 ** 6, 77777)]:
+        for a, b in ((nl, ns), (ns, nl)):
+            plan = _lib.chunk_plan(a, b)
+            assert plan is not None, (a, b)
+            L, c, k = plan
+            T = 1 << L
+            assert c % 8 == 0 and 2 * c >= T and c + ns <= T, plan
+            assert (k - 1) * c < nl <= k * c and k >= 2, plan
+            assert L < (nl + ns - 1).bit_length(), plan
+            seen.add(L)
+    assert any(L <= 12 for L in seen) and any(L > 12 for L in seen)
+
+
 def test_no_cpu_fallback_without_gpu(lib):
     """Without a GPU the product entry points fail loudly."""
     try:
