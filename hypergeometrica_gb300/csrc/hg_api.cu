@@ -98,20 +98,6 @@ std::vector<uint64_t> default_moduli_h() {
   return v;
 }
 
-// The products' primes: the three largest c*2^55 + 1 below 2^62 (c = 116,
-// 69, 57), largest first.  4p < 2^64 lets the butterflies run lazily; each
-// product coefficient (below min(nx, ny) 2^128 < 2^157) is far below their
-// product (about 2^183.8), so the reconstruction is exact and the result is
-// the integer the reference's moduli give.
-std::vector<uint64_t> product_moduli_h() {
-  std::vector<uint64_t> v;
-  for (uint64_t c = 127; c >= 1 && v.size() < kPrimes; --c) {
-    const uint64_t p = (c << kShift) + 1;
-    if (isprime_h(p)) v.push_back(p);
-  }
-  return v;
-}
-
 // ---- context -----------------------------------------------------------
 struct DevBuf {
   void *p = nullptr;
@@ -136,15 +122,10 @@ struct DevBuf {
 struct Context {
   bool ready = false;
   int device = 0;
-  // The reference's scheme (spectrum entry points, canonical butterflies).
   uint64_t moduli[kPrimes] = {};
   uint64_t gens[kPrimes] = {};
   PrimeConst pc[kPrimes] = {};
   NttTables tb[kPrimes] = {};
-  // The products' primes (lazy butterflies).
-  uint64_t qmod[kPrimes] = {};
-  PrimeConst qpc[kPrimes] = {};
-  NttTables qtb[kPrimes] = {};
   DevBuf tables;
   cudaStream_t stream = nullptr;
   DevBuf A, B, X, Y, OUT, flags;
@@ -254,29 +235,17 @@ int init_locked(const uint64_t *moduli, int k, int device) {
   }
   if (device >= 0) HG_CUDA(cudaSetDevice(device), "cudaSetDevice");
   HG_CUDA(cudaGetDevice(&c.device), "cudaGetDevice");
-  const std::vector<uint64_t> qm = product_moduli_h();
-  if (qm.size() != kPrimes) return fail(HG_ERR_NOT_INIT, "expected %d product moduli, found %zu", kPrimes, qm.size());
-  // Tables of prime j (j < kPrimes: the scheme's, then the products').
-  std::vector<uint64_t> host(kPrimeTableWords * 2 * kPrimes);
-  for (int j = 0; j < 2 * kPrimes; ++j) {
-    const bool scheme = j < kPrimes;
-    const int i = scheme ? j : j - kPrimes;
-    const uint64_t p = scheme ? dm[i] : qm[i];
-    const uint64_t g = generator_h(p);
-    const PrimeConst pc{p, static_cast<uint32_t>(p >> kShift), 0, static_cast<uint64_t>((u128(1) << 64) / p)};
-    if (scheme) {
-      c.moduli[i] = p;
-      c.gens[i] = g;
-      c.pc[i] = pc;
-    } else {
-      c.qmod[i] = p;
-      c.qpc[i] = pc;
-    }
-    const uint64_t w30 = powmod_h(g, (p - 1) >> kLogNmax, p);
+  std::vector<uint64_t> host(kPrimeTableWords * kPrimes);
+  for (int i = 0; i < kPrimes; ++i) {
+    const uint64_t p = dm[i];
+    c.moduli[i] = p;
+    c.pc[i] = PrimeConst{p, static_cast<uint32_t>(p >> kShift), 0};
+    c.gens[i] = generator_h(p);
+    const uint64_t w30 = powmod_h(c.gens[i], (p - 1) >> kLogNmax, p);
     const uint64_t w30i = invmod_h(w30, p);
     const uint64_t w4096 = powmod_h(w30, uint64_t(1) << (kLogNmax - kTileBits), p);
     const uint64_t w4096i = invmod_h(w4096, p);
-    uint64_t *t = host.data() + j * kPrimeTableWords;
+    uint64_t *t = host.data() + i * kPrimeTableWords;
     uint64_t *sub_f = t, *sub_i = t + kSubWords, *hi_f = t + 2 * kSubWords, *lo_f = hi_f + kLevelWords,
              *hi_i = lo_f + kLevelWords, *lo_i = hi_i + kLevelWords;
     uint64_t a = 1, b = 1;
@@ -300,9 +269,13 @@ int init_locked(const uint64_t *moduli, int k, int device) {
       hf = mulmod_h(hf, step_f, p);
       hi = mulmod_h(hi, step_i, p);
     }
-    // Per block size 2^T, the sub-transform tables in swizzled order, copied
-    // from the 4096-point tables above (entry e of the table of T is entry
-    // e * 2^(12 - T) of the 4096-point one).
+  }
+  // Per block size 2^T, the sub-transform tables in swizzled order, copied
+  // from the 4096-point tables above (entry e of the table of T is entry
+  // e * 2^(12 - T) of the 4096-point one).
+  for (int i = 0; i < kPrimes; ++i) {
+    uint64_t *t = host.data() + i * kPrimeTableWords;
+    const uint64_t *sub_f = t, *sub_i = t + kSubWords;
     uint64_t *swz = t + 2 * kSubWords + 4 * kLevelWords;
     for (int T = 1; T <= kTileBits; ++T) {
       const uint32_t base = (1u << (T - 1)) - 1u;
@@ -317,16 +290,15 @@ int init_locked(const uint64_t *moduli, int k, int device) {
   }
   HG_CUDA(c.tables.ensure(host.size() * sizeof(uint64_t)), "table allocation");
   HG_CUDA(cudaMemcpy(c.tables.p, host.data(), host.size() * sizeof(uint64_t), cudaMemcpyHostToDevice), "table upload");
-  for (int j = 0; j < 2 * kPrimes; ++j) {
-    const uint64_t *t = c.tables.u64() + j * kPrimeTableWords;
-    NttTables &tb = j < kPrimes ? c.tb[j] : c.qtb[j - kPrimes];
-    tb.sub_fwd = reinterpret_cast<const ulonglong2 *>(t);
-    tb.sub_inv = reinterpret_cast<const ulonglong2 *>(t + kSubWords);
-    tb.hi_fwd = t + 2 * kSubWords;
-    tb.lo_fwd = tb.hi_fwd + kLevelWords;
-    tb.hi_inv = tb.lo_fwd + kLevelWords;
-    tb.lo_inv = tb.hi_inv + kLevelWords;
-    tb.swz = reinterpret_cast<const ulonglong2 *>(t + 2 * kSubWords + 4 * kLevelWords);
+  for (int i = 0; i < kPrimes; ++i) {
+    const uint64_t *t = c.tables.u64() + i * kPrimeTableWords;
+    c.tb[i].sub_fwd = reinterpret_cast<const ulonglong2 *>(t);
+    c.tb[i].sub_inv = reinterpret_cast<const ulonglong2 *>(t + kSubWords);
+    c.tb[i].hi_fwd = t + 2 * kSubWords;
+    c.tb[i].lo_fwd = c.tb[i].hi_fwd + kLevelWords;
+    c.tb[i].hi_inv = c.tb[i].lo_fwd + kLevelWords;
+    c.tb[i].lo_inv = c.tb[i].hi_inv + kLevelWords;
+    c.tb[i].swz = reinterpret_cast<const ulonglong2 *>(t + 2 * kSubWords + 4 * kLevelWords);
   }
   HG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream creation");
   HG_CUDA(cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming), "event creation");
@@ -380,10 +352,8 @@ std::vector<PassPlan> plan_passes(int L) {
   return v;
 }
 
-// Arguments of a product's passes: the products' primes, lazy butterflies.
 PassArgs base_args(int L, int nops) {
   PassArgs a{};
-  a.lazy = 1;
   a.nops = nops;
   a.logN = L;
   a.prime_lo = 0;
@@ -392,8 +362,8 @@ PassArgs base_args(int L, int nops) {
   a.nprod = 1;
   a.ws_stride = static_cast<uint64_t>(kPrimes) << L;
   for (int i = 0; i < kPrimes; ++i) {
-    a.pc[i] = g_ctx.qpc[i];
-    a.tb[i] = g_ctx.qtb[i];
+    a.pc[i] = g_ctx.pc[i];
+    a.tb[i] = g_ctx.tb[i];
   }
   return a;
 }
@@ -442,7 +412,7 @@ const uint64_t *pass_twiddles(int logM, int logR, bool inverse, cudaStream_t st)
   }
   cudaStream_t bs = nullptr;
   if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess ||
-      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.qtb, g_ctx.qpc, kPrimes, bs) != cudaSuccess ||
+      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, bs) != cudaSuccess ||
       cudaStreamSynchronize(bs) != cudaSuccess) {
     if (bs) cudaStreamDestroy(bs);
     cudaGetLastError();
@@ -472,8 +442,7 @@ cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, boo
     a.logS = pp.logS;
     a.logT = pp.logT;
     a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
-    // The tables hold the products' primes; the spectrum passes form theirs.
-    a.ptw = a.lazy ? pass_twiddles(pp.logR + pp.logS, pp.logR, inverse, st) : nullptr;
+    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse, st);
     cudaError_t e;
     {
       ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, pass_bytes(a, a.nops, a.nops));
@@ -505,8 +474,8 @@ cudaError_t run_contig(PassArgs a, const PassPlan &pp, int mode, cudaStream_t st
 
 CrtConst crt_const(int L) {
   CrtConst k{};
-  const uint64_t p0 = g_ctx.qmod[0], p1 = g_ctx.qmod[1], p2 = g_ctx.qmod[2];
-  for (int i = 0; i < kPrimes; ++i) k.pc[i] = g_ctx.qpc[i];
+  const uint64_t p0 = g_ctx.moduli[0], p1 = g_ctx.moduli[1], p2 = g_ctx.moduli[2];
+  for (int i = 0; i < kPrimes; ++i) k.pc[i] = g_ctx.pc[i];
   const uint64_t N = uint64_t(1) << L;
   const uint64_t n0 = invmod_h(N % p0, p0), n1 = invmod_h(N % p1, p1), n2 = invmod_h(N % p2, p2);
   const uint64_t R0 = mont_h(1, p0), R1 = mont_h(1, p1), R2 = mont_h(1, p2);  // 2^64 mod p
@@ -1007,14 +976,7 @@ int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) 
   const int L = ilog2_ceil(n);
   rc = check_len(L);
   if (rc) return rc;
-  // The reference's primes with canonical butterflies (ntt-forward and
-  // ntt-reverse leave every residue in [0, p)).
   PassArgs pa = base_args(L, 1);
-  pa.lazy = 0;
-  for (int i = 0; i < kPrimes; ++i) {
-    pa.pc[i] = g_ctx.pc[i];
-    pa.tb[i] = g_ctx.tb[i];
-  }
   pa.data[0] = a;
   pa.prime_lo = mod_num;
   pa.nprimes = 1;
@@ -1537,7 +1499,7 @@ int hg_butterfly_peak(double *butterflies_per_s) {
   int rc = ensure_init();
   if (rc) return rc;
   if (!butterflies_per_s) return fail(HG_ERR_ARG, "null pointer");
-  return butterfly_peak(butterflies_per_s, g_ctx.qpc[0], g_ctx.qtb[0].sub_fwd);
+  return butterfly_peak(butterflies_per_s, g_ctx.pc[0], g_ctx.tb[0].sub_fwd);
 }
 
 int hg_sync(void *stream) {

@@ -1,17 +1,8 @@
 // hg_common.cuh -- shared definitions of the GB300 multiplication library.
 //
-// Two sets of primes p = c * 2^55 + 1.  The spectrum entry points transform
-// modulo the reference's three NTT primes (default-moduli,
-// src/moduli.lisp:257-264; c = 197, 174, 131, all above 2^62) with every
-// residue kept in [0, p), exactly as ntt-forward / ntt-reverse do.  Products
-// run modulo three primes of the same shape below 2^62 (c = 116, 69, 57):
-// with 4p < 2^64 the butterflies may leave residues in [0, 2p) (forward) or
-// [0, 4p) (inverse) and skip most corrections.  The product is the same
-// integer either way: each convolution coefficient is below
-// min(nx, ny) * 2^128 < 2^157, far below either set's modulus product, so
-// it has one representation.
-//
-// The shape makes Montgomery reduction with R = 2^64 cheap: p^-1 mod 2^64 is
+// Arithmetic is modulo the reference's three NTT primes (default-moduli,
+// src/moduli.lisp:257-264): p = c * 2^55 + 1 with c = 197, 174, 131.  That
+// shape makes Montgomery reduction with R = 2^64 cheap: p^-1 mod 2^64 is
 // 1 - c*2^55, and floor(m*p / 2^64) needs only a 64 x 8-bit product.  The
 // reference's Barrett (m*/fast, src/modular-arithmetic.lisp:167-202) and
 // Shoup (m*/fast2, :207-231) multiplications compute the same residues; only
@@ -38,7 +29,6 @@ struct PrimeConst {
   uint64_t p;
   uint32_t c;  // p = c * 2^55 + 1
   uint32_t pad;
-  uint64_t one_q;  // floor(2^64 / p): the Shoup companion of 1
 };
 
 // Device error word codes (latched with atomicCAS; first error wins).
@@ -63,8 +53,7 @@ __host__ __device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uin
 
 __device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __umul64hi(a, b); }
 
-// Montgomery product a * b * 2^-64 mod p, for a * b < p * 2^64 (any 64-bit
-// a and b < p; or a, b < 2p, a < 4p and b < p when 4p < 2^64), with
+// Montgomery product a * b * 2^-64 mod p, for any 64-bit a and b < p, with
 // p = c * 2^55 + 1.  Result is fully reduced in [0, p).
 //   m = lo * p^-1 mod 2^64 = lo - ((lo * c) mod 2^9) * 2^55   (m1:m0 below)
 //   floor(m * p / 2^64) = u * 2^23 + floor((t mod 2^32) / 2^9) with
@@ -73,7 +62,7 @@ __device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __
 // them off the integer ALU pipe that the butterflies' additions load.
 __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p, uint32_t c) {
   const uint64_t lo = a * b;
-  const uint64_t hi = mul_hi64(a, b);  // < p because a * b < p * 2^64
+  const uint64_t hi = mul_hi64(a, b);  // < p because a < 2^64 and b < p
   const uint32_t m0 = static_cast<uint32_t>(lo);
   const uint32_t m1 = static_cast<uint32_t>(lo >> 32) - m0 * (c << 23);
   uint64_t t;
@@ -105,21 +94,11 @@ __device__ __forceinline__ uint64_t shoup_mul(uint64_t a, uint64_t w, uint64_t w
   return r >= p ? r - p : r;
 }
 
-// Shoup product without the final correction: a * w mod p in [0, 2p), for
-// any 64-bit a and w < p < 2^63 with companion wq.
-__device__ __forceinline__ uint64_t shoup_lazy(uint64_t a, uint64_t w, uint64_t wq, uint32_t c) {
-  const uint64_t q = mul_hi64(a, wq);
-  return a * w - q - (static_cast<uint64_t>(static_cast<uint32_t>(q) * (c << 23)) << 32);
-}
-
-// A limb (any 64-bit x) modulo p: x * 1 by Shoup, in [0, 2p) ...
-__device__ __forceinline__ uint64_t reduce_lazy(uint64_t x, const PrimeConst &pc) {
-  return shoup_lazy(x, 1, pc.one_q, pc.c);
-}
-// ... or in [0, p).
-__device__ __forceinline__ uint64_t reduce_full(uint64_t x, const PrimeConst &pc) {
-  const uint64_t r = reduce_lazy(x, pc);
-  return r >= pc.p ? r - pc.p : r;
+// x mod p for any 64-bit x (x < 4p because p > 2^62).
+__device__ __forceinline__ uint64_t reduce64(uint64_t x, uint64_t p) {
+  const uint64_t p2 = p << 1;
+  if (x >= p2) x -= p2;
+  return x >= p ? x - p : x;
 }
 
 // Carry-lookahead pair for the final carry scan: with carry-in c, a

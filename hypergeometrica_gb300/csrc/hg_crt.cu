@@ -73,8 +73,6 @@ struct CrtProducer {
     }
   }
 
-  // Residues may be any 64-bit values congruent to the coefficient (the lazy
-  // inverse leaves [0, 4p)): every one enters through a Shoup product.
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
@@ -102,21 +100,16 @@ struct CrtProducer {
 // 2^(logN-1) makes at most two chunks meet at a position.  Their residues
 // are added before the reconstruction: the sum of the two coefficients is
 // below 2 * short * 2^128, far below p0 p1 p2, so Garner's value of the
-// summed residues is the exact sum.  The lazy inverse leaves residues in
-// [0, 4p); each is folded to [0, 2p) and the sum, below 4p, goes to Garner,
-// whose Shoup products take any 64-bit residue.
+// summed residues is the exact sum.
 struct ChunkProducer {
   CrtProducer crt;      // res = chunk 0's residues, n = 2^logN
   uint64_t stride;      // words between consecutive chunks' residues
   uint64_t chunk, nchunks;
 
-  __device__ __forceinline__ static uint64_t sum2(uint64_t a, uint64_t b, uint64_t p2) {
-    return (a >= p2 ? a - p2 : a) + (b >= p2 ? b - p2 : b);
-  }
-
   __device__ __forceinline__ uint64_t sum_res(const uint64_t *r0, const uint64_t *r1, int j) const {
+    const uint64_t p = crt.k.pc[j].p;
     const uint64_t a = r0 ? r0[j * crt.n] : 0, b = r1 ? r1[j * crt.n] : 0;
-    return sum2(a, b, crt.k.pc[j].p << 1);
+    return add_mod(a, b, p);
   }
 
   // Residue pointers of position i: the chunk that starts at or below i, and
@@ -145,14 +138,14 @@ struct ChunkProducer {
     uint64_t r[3][8];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const uint64_t p2 = crt.k.pc[j].p << 1;
+      const uint64_t p = crt.k.pc[j].p;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         ulonglong2 a = make_ulonglong2(0, 0), b = make_ulonglong2(0, 0);
         if (r0) a = __ldg(reinterpret_cast<const ulonglong2 *>(r0 + j * crt.n) + q);
         if (r1) b = __ldg(reinterpret_cast<const ulonglong2 *>(r1 + j * crt.n) + q);
-        r[j][2 * q] = sum2(a.x, b.x, p2);
-        r[j][2 * q + 1] = sum2(a.y, b.y, p2);
+        r[j][2 * q] = add_mod(a.x, b.x, p);
+        r[j][2 * q + 1] = add_mod(a.y, b.y, p);
       }
     }
 #pragma unroll

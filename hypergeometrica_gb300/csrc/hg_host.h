@@ -66,9 +66,9 @@ int lib_cuda_fail(cudaError_t e, const char *what);
 // Count of open services; hg_shutdown refuses while it is nonzero.
 void lib_service_count(int delta);
 
-// Butterflies per second of a memory-free network of the library's lazy
-// modular butterflies (hg_peak.cu), with a product prime pc (below 2^62)
-// and a device table of at least 1024 (twiddle, companion) pairs.
+// Butterflies per second of a memory-free network of the library's modular
+// butterflies (hg_peak.cu), with prime pc and a device table of at least
+// 1024 (twiddle, companion) pairs.
 int butterfly_peak(double *per_s, const PrimeConst &pc, const ulonglong2 *table);
 
 }  // namespace hg

@@ -53,8 +53,6 @@ struct PassArgs {
   uint64_t chunk;              // single product cut into chunks: product k reads
                                // operand 0's limbs [k * chunk, (k + 1) * chunk)
   int read_limbs;              // batch: this pass reads and reduces limbs
-  int lazy;                    // products: lazy butterflies (primes below 2^62);
-                               // 0: every residue in [0, p) (spectrum entry points)
   int nops;                    // operands handled by this launch
   int logN;
   int logR;                    // log2 rows (transform points) of this pass

@@ -44,14 +44,14 @@ struct Groups {
   __host__ __device__ static constexpr int JG() { return 4 - NB<g>(); }
 };
 
-template <int T, int g, bool INV, bool LAZY>
+template <int T, int g, bool INV>
 __device__ __forceinline__ void round_g(uint64_t (&v)[16], const ulonglong2 *tw, uint32_t xt, uint64_t p, uint32_t c) {
   using Gr = Groups<T>;
   constexpr int A = Gr::template A<g>();
   constexpr int NB = Gr::template NB<g>();
   constexpr int JG = Gr::template JG<g>();
   constexpr bool TZERO = (g == 0) && (A == 0) && (JG == 0);
-  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO, LAZY>(v, tw, xt, p, c);
+  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO>(v, tw, xt, p, c);
 }
 
 // Move the thread's registers from the layout of group g to that of group h
@@ -69,50 +69,49 @@ __device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_
 }
 
 // All forward rounds, from the top group down to group 0.
-template <int T, bool LAZY>
+template <int T>
 __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
   if constexpr (G == 3) {
-    round_g<T, 2, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 2, false>(v, tw, xt, p, c);
     regroup<T, 2, 1>(v, sm, xt, tid);
-    round_g<T, 1, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 1, false>(v, tw, xt, p, c);
     regroup<T, 1, 0>(v, sm, xt, tid);
-    round_g<T, 0, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 0, false>(v, tw, xt, p, c);
   } else if constexpr (G == 2) {
-    round_g<T, 1, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 1, false>(v, tw, xt, p, c);
     regroup<T, 1, 0>(v, sm, xt, tid);
-    round_g<T, 0, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 0, false>(v, tw, xt, p, c);
   } else {
-    round_g<T, 0, false, LAZY>(v, tw, xt, p, c);
+    round_g<T, 0, false>(v, tw, xt, p, c);
   }
 }
 
 // All inverse rounds, from group 0 up to the top group.
-template <int T, bool LAZY>
+template <int T>
 __device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
-  round_g<T, 0, true, LAZY>(v, tw, xt, p, c);
+  round_g<T, 0, true>(v, tw, xt, p, c);
   if constexpr (G >= 2) {
     regroup<T, 0, 1>(v, sm, xt, tid);
-    round_g<T, 1, true, LAZY>(v, tw, xt, p, c);
+    round_g<T, 1, true>(v, tw, xt, p, c);
   }
   if constexpr (G == 3) {
     regroup<T, 1, 2>(v, sm, xt, tid);
-    round_g<T, 2, true, LAZY>(v, tw, xt, p, c);
+    round_g<T, 2, true>(v, tw, xt, p, c);
   }
 }
 
-template <int A, bool LAZY>
+template <int A>
 __device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *data, const uint64_t *limbs, uint64_t nl,
-                                           uint64_t base, uint32_t xt, const PrimeConst &pc) {
+                                           uint64_t base, uint32_t xt, uint64_t p) {
   if (limbs) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const uint64_t o = base + (xt | (static_cast<uint32_t>(i) << A));
-      const uint64_t x = o < nl ? __ldg(limbs + o) : 0;
-      v[i] = LAZY ? reduce_lazy(x, pc) : reduce_full(x, pc);
+      v[i] = o < nl ? reduce64(__ldg(limbs + o), p) : 0;
     }
   } else {
 #pragma unroll
@@ -135,7 +134,7 @@ __device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *d
 // without spilling, two (128 registers) for the 9..11-bit blocks.
 __host__ __device__ constexpr int contig_min_blocks(int T) { return (T >= 9 && T <= 11) ? 2 : 3; }
 
-template <int T, int MODE, bool LAZY>
+template <int T, int MODE>
 __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig_kernel(const PassArgs P) {
   using Gr = Groups<T>;
   constexpr int ATOP = Gr::template A<Gr::G - 1>();
@@ -174,30 +173,30 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
   uint32_t xt;
   if constexpr (MODE == kInv) {
     xt = thread_base<A0>(lt);
-    if (valid) load_block<A0, LAZY>(v, P.data[0] + poff, nullptr, 0, base, xt, P.pc[prime]);
+    if (valid) load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
     else zero16(v);
-    inverse_rounds<T, LAZY>(v, smA, tw, xt, lt, p, c);
+    inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
   } else if constexpr (MODE == kFwd) {
     xt = thread_base<ATOP>(lt);
-    if (valid) load_block<ATOP, LAZY>(v, P.data[0] + poff, limbs0, nl0, base, xt, P.pc[prime]);
+    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
     else zero16(v);
-    forward_rounds<T, LAZY>(v, smA, tw, xt, lt, p, c);
+    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
     if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
     return;
   } else if constexpr (MODE == kMulSpec) {
     xt = thread_base<ATOP>(lt);
-    if (valid) load_block<ATOP, LAZY>(v, P.data[0] + poff, limbs0, nl0, base, xt, P.pc[prime]);
+    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
     else zero16(v);
-    forward_rounds<T, LAZY>(v, smA, tw, xt, lt, p, c);
+    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
     // The shared spectrum sits where kFwd stores it, without a product offset.
     if (valid) {
       const uint64_t *spec = P.data[1] + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride + base;
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(spec + (xt | (static_cast<uint32_t>(i) << A0))), p, c);
     }
-    inverse_rounds<T, LAZY>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
+    inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
     if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
   } else {
@@ -209,10 +208,9 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
 #pragma unroll 1
       for (int op = 0; op < nop; ++op) {
         xt = thread_base<ATOP>(lt);
-        if (valid)
-          load_block<ATOP, LAZY>(v, P.data[op] + poff, op ? limbs1 : limbs0, op ? nl1 : nl0, base, xt, P.pc[prime]);
+        if (valid) load_block<ATOP>(v, P.data[op] + poff, op ? limbs1 : limbs0, op ? nl1 : nl0, base, xt, p);
         else zero16(v);
-        forward_rounds<T, LAZY>(v, op ? smB : smA, tw, xt, lt, p, c);
+        forward_rounds<T>(v, op ? smB : smA, tw, xt, lt, p, c);
         if (TWO && op == 0) {
           __syncthreads();
           to_smem<A0>(smA, v, xt);
@@ -229,7 +227,7 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
-      inverse_rounds<T, LAZY>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
+      inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
       if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     }
   }
@@ -252,8 +250,7 @@ __global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
     uint64_t nl = 0;
     const uint64_t *limbs = pass_limbs(P, prod, op, nl);
     for (int i = 0; i < n; ++i)
-      a[op][i] = limbs ? (static_cast<uint64_t>(i) < nl ? reduce_full(limbs[i], P.pc[prime]) : 0)
-                       : P.data[op][poff + i];
+      a[op][i] = limbs ? (static_cast<uint64_t>(i) < nl ? reduce64(limbs[i], p) : 0) : P.data[op][poff + i];
   }
   if (mode != kInv) {
     for (int op = 0; op < nops; ++op)
@@ -293,7 +290,7 @@ __global__ void scale_kernel(uint64_t *a, uint64_t n, uint64_t f, uint64_t p, ui
     a[i] = mont_mul(a[i], f, p, c);
 }
 
-template <int T, int MODE, bool LAZY>
+template <int T, int MODE>
 cudaError_t launch_tm(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
   constexpr uint64_t bpc = uint64_t(1) << (kTileBits - T);
   constexpr size_t bytes = static_cast<size_t>(MODE == kMul ? 2 : 1) * (1u << kTileBits) * sizeof(uint64_t);
@@ -304,27 +301,27 @@ cudaError_t launch_tm(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
   // every launch, so that launches can be captured in a CUDA graph).
   static bool raised = false;
   if (bytes > 48 * 1024 && !raised) {
-    cudaError_t e = cudaFuncSetAttribute(ntt_contig_kernel<T, MODE, LAZY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(ntt_contig_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(bytes));
     if (e != cudaSuccess) return e;
     raised = true;
   }
-  ntt_contig_kernel<T, MODE, LAZY><<<grid, kTileThreads, bytes, st>>>(a);
+  ntt_contig_kernel<T, MODE><<<grid, kTileThreads, bytes, st>>>(a);
   return cudaGetLastError();
 }
 
-template <int MODE, bool LAZY>
+template <int MODE>
 cudaError_t launch_mode(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
   switch (a.logT) {
-    case 4: return launch_tm<4, MODE, LAZY>(a, nblk, st);
-    case 5: return launch_tm<5, MODE, LAZY>(a, nblk, st);
-    case 6: return launch_tm<6, MODE, LAZY>(a, nblk, st);
-    case 7: return launch_tm<7, MODE, LAZY>(a, nblk, st);
-    case 8: return launch_tm<8, MODE, LAZY>(a, nblk, st);
-    case 9: return launch_tm<9, MODE, LAZY>(a, nblk, st);
-    case 10: return launch_tm<10, MODE, LAZY>(a, nblk, st);
-    case 11: return launch_tm<11, MODE, LAZY>(a, nblk, st);
-    case 12: return launch_tm<12, MODE, LAZY>(a, nblk, st);
+    case 4: return launch_tm<4, MODE>(a, nblk, st);
+    case 5: return launch_tm<5, MODE>(a, nblk, st);
+    case 6: return launch_tm<6, MODE>(a, nblk, st);
+    case 7: return launch_tm<7, MODE>(a, nblk, st);
+    case 8: return launch_tm<8, MODE>(a, nblk, st);
+    case 9: return launch_tm<9, MODE>(a, nblk, st);
+    case 10: return launch_tm<10, MODE>(a, nblk, st);
+    case 11: return launch_tm<11, MODE>(a, nblk, st);
+    case 12: return launch_tm<12, MODE>(a, nblk, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -340,14 +337,12 @@ cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
     ntt_tiny_kernel<<<dim3(static_cast<unsigned>(a.nprod), static_cast<unsigned>(a.nprimes)), 1, 0, st>>>(a, mode);
     return cudaGetLastError();
   }
-  // Products run lazy (their forward passes and middles); the spectrum entry
-  // points run canonical forward and inverse passes.
   switch (mode) {
-    case kFwd: return a.lazy ? launch_mode<kFwd, true>(a, nblk, st) : launch_mode<kFwd, false>(a, nblk, st);
-    case kInv: return a.lazy ? cudaErrorInvalidValue : launch_mode<kInv, false>(a, nblk, st);
-    case kMul: return a.lazy ? launch_mode<kMul, true>(a, nblk, st) : cudaErrorInvalidValue;
-    case kSqr: return a.lazy ? launch_mode<kSqr, true>(a, nblk, st) : cudaErrorInvalidValue;
-    case kMulSpec: return a.lazy ? launch_mode<kMulSpec, true>(a, nblk, st) : cudaErrorInvalidValue;
+    case kFwd: return launch_mode<kFwd>(a, nblk, st);
+    case kInv: return launch_mode<kInv>(a, nblk, st);
+    case kMul: return launch_mode<kMul>(a, nblk, st);
+    case kSqr: return launch_mode<kSqr>(a, nblk, st);
+    case kMulSpec: return launch_mode<kMulSpec>(a, nblk, st);
     default: return cudaErrorInvalidValue;
   }
 }

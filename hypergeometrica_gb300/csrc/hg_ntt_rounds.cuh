@@ -62,17 +62,9 @@ __device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const ui
 // the thread's row bits below b (runtime, zero when TZERO) and the register's
 // (compile time).  With TZERO, butterflies whose twiddle is 1 skip the
 // multiplication.
-//
-// Canonical (LAZY false): inputs and outputs in [0, p), the reference's
-// butterflies.  LAZY (4p < 2^64): the forward (DIF) butterfly takes and
-// leaves [0, 2p) -- u + v folded once by 2p, (u - v + 2p) w by Shoup without
-// its correction; the inverse (DIT) butterfly takes and leaves [0, 4p) -- u
-// folded to [0, 2p), v w by Shoup without correction (v folded when w = 1),
-// then u + t and u - t + 2p.
-template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO, bool LAZY>
+template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO>
 __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__restrict__ tw, uint32_t xt, uint64_t p,
                                        uint32_t c) {
-  const uint64_t p2 = p << 1;
 #pragma unroll
   for (int s = 0; s < NB; ++s) {
     const int jj = INV ? s : NB - 1 - s;
@@ -87,31 +79,6 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__re
       const uint32_t rp = ((static_cast<uint32_t>(i) << A) >> ROWOFF) & lowmask;
       const bool trivial = TZERO && rp == 0;
       const uint64_t u = v[i], w = v[i | (1 << j)];
-      if constexpr (LAZY) {
-        if (!INV) {
-          const uint64_t s2 = u + w;
-          v[i] = s2 >= p2 ? s2 - p2 : s2;
-          const uint64_t d = u - w + p2;  // (0, 4p)
-          if (trivial) {
-            v[i | (1 << j)] = d >= p2 ? d - p2 : d;
-          } else {
-            const ulonglong2 t = tw[ts ^ swz_tw(rp << sh)];
-            v[i | (1 << j)] = shoup_lazy(d, t.x, t.y, c);
-          }
-        } else {
-          const uint64_t uu = u >= p2 ? u - p2 : u;
-          uint64_t t;
-          if (trivial) {
-            t = w >= p2 ? w - p2 : w;
-          } else {
-            const ulonglong2 tt = tw[ts ^ swz_tw(rp << sh)];
-            t = shoup_lazy(w, tt.x, tt.y, c);
-          }
-          v[i] = uu + t;
-          v[i | (1 << j)] = uu - t + p2;
-        }
-        continue;
-      }
       if (!INV) {
         v[i] = add_mod(u, w, p);
         if (trivial) {

@@ -17,10 +17,6 @@
 // once through shared memory, runs the stages of the low four row bits, and
 // applies the inter-pass twiddle to its 16 rows of one column as a geometric
 // sequence beta * gamma^k before storing from registers.
-//
-// Products run the lazy butterflies (LAZY): a forward pass leaves residues in
-// [0, p) (the inter-pass twiddle's Montgomery product reduces them), an
-// inverse pass reads [0, 4p) and leaves [0, 4p).
 #include <algorithm>
 
 #include "hg_ntt_rounds.cuh"
@@ -33,7 +29,7 @@ using namespace rounds;
 // Four CTAs of 256 threads per SM (64 registers, a few spilled words): on
 // the 2^25-point passes faster than three (80 registers), two (128) or five
 // (48).
-template <int LOGR, bool INV, bool LAZY>
+template <int LOGR, bool INV>
 __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const PassArgs P) {
   constexpr int T = kTileBits;
   constexpr int LOGTC = T - LOGR;  // log2 columns per tile
@@ -106,8 +102,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const uint64_t o = off + i * step;
-        const uint64_t x = o < nl ? __ldg(limbs + o) : 0;
-        v[i] = LAZY ? reduce_lazy(x, P.pc[prime]) : reduce_full(x, P.pc[prime]);
+        v[i] = o < nl ? reduce64(__ldg(limbs + o), p) : 0;
       }
     } else {
 #pragma unroll
@@ -115,13 +110,13 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
     }
     __syncthreads();  // twiddle table ready
     if constexpr (G == 2) {
-      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false, LAZY>(v, tw, xt, p, c);
+      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false>(v, tw, xt, p, c);
       to_smem<A1>(sm, v, xt);
       __syncthreads();
       xt = thread_base<A0>(tid);
       from_smem<A0>(v, sm, xt);
     }
-    stages<4, 0, A0, ROWOFF, 0, LOGR, false, true, LAZY>(v, tw, xt, p, c);
+    stages<4, 0, A0, ROWOFF, 0, LOGR, false, true>(v, tw, xt, p, c);
     inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
     offsets(xt, A0, off, step);
 #pragma unroll
@@ -134,13 +129,13 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
     for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
     inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
     __syncthreads();  // twiddle table ready
-    stages<4, 0, A0, ROWOFF, 0, LOGR, true, true, LAZY>(v, tw, xt, p, c);
+    stages<4, 0, A0, ROWOFF, 0, LOGR, true, true>(v, tw, xt, p, c);
     if constexpr (G == 2) {
       to_smem<A0>(sm, v, xt);
       __syncthreads();
       xt = thread_base<A1>(tid);
       from_smem<A1>(v, sm, xt);
-      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, true, false, LAZY>(v, tw, xt, p, c);
+      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, true, false>(v, tw, xt, p, c);
       offsets(xt, A1, off, step);
     }
 #pragma unroll
@@ -166,17 +161,10 @@ __global__ void pass_twiddles_kernel(uint64_t *out, int logM, int logR, bool inv
 
 template <int LOGR>
 cudaError_t launch_r(const PassArgs &a, bool inverse, unsigned grid, cudaStream_t st) {
-  if (a.lazy) {
-    if (inverse)
-      ntt_strided_kernel<LOGR, true, true><<<grid, kTileThreads, 0, st>>>(a);
-    else
-      ntt_strided_kernel<LOGR, false, true><<<grid, kTileThreads, 0, st>>>(a);
-  } else {
-    if (inverse)
-      ntt_strided_kernel<LOGR, true, false><<<grid, kTileThreads, 0, st>>>(a);
-    else
-      ntt_strided_kernel<LOGR, false, false><<<grid, kTileThreads, 0, st>>>(a);
-  }
+  if (inverse)
+    ntt_strided_kernel<LOGR, true><<<grid, kTileThreads, 0, st>>>(a);
+  else
+    ntt_strided_kernel<LOGR, false><<<grid, kTileThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

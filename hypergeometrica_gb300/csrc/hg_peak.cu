@@ -1,14 +1,13 @@
 // hg_peak.cu -- the integer-pipe ceiling of the modular butterflies.
 //
 // The NTT passes are bound by the integer pipes, not by HBM: each radix-2
-// butterfly is a 64-bit addition, a subtraction, their folds and a Shoup
-// product built from 32-bit IMAD and ALU instructions.  This kernel runs the
-// products' lazy butterflies (the LAZY branch of hg_ntt_rounds.cuh's stages,
-// with a product prime below 2^62) on 16 registers per thread with twiddles
-// from shared memory and no global traffic, half forward (DIF, residues in
-// [0, 2p)) then half inverse (DIT, [0, 4p)), over every SM: its rate is the
-// practical peak a memory-free butterfly network reaches on this GPU, the
-// denominator of the product's integer-pipe roofline.
+// butterfly is a 64-bit modular add, a subtract and a Shoup product built
+// from 32-bit IMAD and ALU instructions.  This kernel runs the same
+// butterflies (hg_common.cuh's add_mod / sub_mod / shoup_mul) on 16
+// registers per thread with twiddles from shared memory and no global
+// traffic, half forward (DIF) and half inverse (DIT), over every SM: its
+// rate is the practical peak a memory-free butterfly network reaches on this
+// GPU, the denominator of the product's integer-pipe roofline.
 #include <cstdio>
 
 #include "hg_host.h"
@@ -23,7 +22,7 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
   __shared__ ulonglong2 tw[16];
   if (threadIdx.x < 16) tw[threadIdx.x] = table[threadIdx.x * 64];
   __syncthreads();
-  const uint64_t p = pc.p, p2 = pc.p << 1;
+  const uint64_t p = pc.p;
   const uint32_t c = pc.c;
   const uint64_t gid = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   uint64_t v[16];
@@ -31,7 +30,7 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
   for (int i = 0; i < 16; ++i) v[i] = (gid * 16 + i) % p;
   const int off = threadIdx.x & 7;
   for (int it = 0; it < kPeakIters; ++it) {
-    const bool dit = it >= kPeakIters / 2;
+    const bool dit = it & 1;
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
 #pragma unroll
@@ -40,14 +39,12 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
         const ulonglong2 t = tw[((i & ((1 << j) - 1)) + off) & 15];
         const uint64_t u = v[i], x = v[i | (1 << j)];
         if (!dit) {
-          const uint64_t s2 = u + x;
-          v[i] = s2 >= p2 ? s2 - p2 : s2;
-          v[i | (1 << j)] = shoup_lazy(u - x + p2, t.x, t.y, c);
+          v[i] = add_mod(u, x, p);
+          v[i | (1 << j)] = shoup_mul(u - x + p, t.x, t.y, p, c);
         } else {
-          const uint64_t uu = u >= p2 ? u - p2 : u;
-          const uint64_t y = shoup_lazy(x, t.x, t.y, c);
-          v[i] = uu + y;
-          v[i | (1 << j)] = uu - y + p2;
+          const uint64_t y = shoup_mul(x, t.x, t.y, p, c);
+          v[i] = add_mod(u, y, p);
+          v[i | (1 << j)] = sub_mod(u, y, p);
         }
       }
     }
