@@ -406,8 +406,13 @@ def run_sweep(stream, peak_gbs: float) -> dict:
         del a, b, o
         torch.cuda.empty_cache()
     # Unbalanced and edge-value products: 2^24 x 2^16, 2^25 x 2^20, 2^20 x 2^6
-    # limbs, uniform, all-ones (the longest carry chains) and 1%-nonzero limbs, through
-    # the NTT product (hg_mul_device, mpz-*/ntt semantics).
+    # limbs, uniform, all-ones (the longest carry chains) and 1%-nonzero limbs,
+    # through the NTT product (hg_mul_device, mpz-*/ntt semantics): as the
+    # library runs them (in chunks against one spectrum of the short operand)
+    # and as the reference's one transform of the least power of two >= nx + ny
+    # points (chunking switched off); both results must agree.
+    from hypergeometrica_gb300 import _lib
+
     out["unbalanced"] = []
     for ka, kb in ((24, 16), (25, 20), (20, 6)):
         na, nb = 1 << ka, 1 << kb
@@ -416,22 +421,34 @@ def run_sweep(stream, peak_gbs: float) -> dict:
             a = torch.from_numpy(xh.view(np.int64)).cuda()
             b = torch.from_numpy(yh.view(np.int64)).cuda()
             o = torch.empty(na + nb, dtype=torch.int64, device="cuda")
+            o1 = torch.empty_like(o)
             reps = max(2, min(10, (1 << 26) // na))
-            for _ in range(2):
-                D.mul(a, b, o, stream=stream)
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            for _ in range(reps):
-                D.mul(a, b, o, stream=stream)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            ms = ev0.elapsed_time(ev1) / reps
-            D.sync(stream)
-            ok = _residue_ok(o.cpu().numpy().view(np.uint64), xh, yh)
+
+            def timed(dst):
+                for _ in range(2):
+                    D.mul(a, b, dst, stream=stream)
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                for _ in range(reps):
+                    D.mul(a, b, dst, stream=stream)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                D.sync(stream)
+                return ev0.elapsed_time(ev1) / reps
+
+            ms = timed(o)
+            _lib.set_chunking(False)
+            try:
+                ms1 = timed(o1)
+            finally:
+                _lib.set_chunking(True)
+            ok = _residue_ok(o.cpu().numpy().view(np.uint64), xh, yh) and bool(torch.equal(o, o1))
             out["unbalanced"].append({"log_sizes": [ka, kb], "dist": dist, "ms": ms,
-                                      "limbs_per_s": (na + nb) / (ms / 1000.0), "correct": ok})
-            del a, b, o
+                                      "limbs_per_s": (na + nb) / (ms / 1000.0),
+                                      "chunk_plan": _lib.chunk_plan(na, nb), "ms_one_transform": ms1,
+                                      "correct": ok})
+            del a, b, o, o1
         torch.cuda.empty_cache()
     out["correct"] = all(line["correct"] for line in out["lines"] + out["unbalanced"])
     return out

@@ -83,6 +83,7 @@ SIGNATURES = {
     "hg_scheme_moduli": (ctypes.c_int, [_u64p, ctypes.c_int]),
     "hg_ntt_length": (_sz, [_sz, _sz]),
     "hg_chunk_plan": (ctypes.c_int, [_sz, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
+    "hg_set_chunking": (ctypes.c_int, [ctypes.c_int]),
     "hg_mul": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
     "hg_sqr": (ctypes.c_int, [_vp, _sz, _vp, _sz]),
     "hg_mul_schoolboy": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
@@ -126,6 +127,12 @@ def chunk_plan(nx: int, ny: int):
     if not load().hg_chunk_plan(nx, ny, ctypes.byref(L), ctypes.byref(c), ctypes.byref(k)):
         return None
     return L.value, c.value, k.value
+
+
+def set_chunking(on: bool) -> bool:
+    """Allow (True) or forbid unbalanced products in chunks; returns the
+    previous setting."""
+    return bool(load().hg_set_chunking(1 if on else 0))
 
 
 KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "middle", "carry", "small", "other"]

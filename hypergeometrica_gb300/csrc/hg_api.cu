@@ -555,8 +555,10 @@ constexpr double kChunkGain = 0.95;
 // C = (2^L - ns) rounded down to a multiple of 8 (>= 2^(L-1) because
 // 2^L >= 2 pow2(ns) >= 16), so that at most two chunk products meet at any
 // position of the result.
+std::atomic<int> g_chunking{1};  // hg_set_chunking
+
 bool plan_chunks(uint64_t nl, uint64_t ns, ChunkPlan &cp) {
-  if (ns == 0 || nl < ns) return false;
+  if (ns == 0 || nl < ns || !g_chunking.load()) return false;
   const int Lf = ilog2_ceil(nl + ns);
   const auto cost = [](double transforms, int L) { return transforms * std::ldexp(L + kPassCost, L); };
   double best = kChunkGain * cost(3.0, Lf);
@@ -1406,6 +1408,8 @@ int hg_chunk_plan(size_t nx, size_t ny, int *log_len, size_t *chunk, size_t *nch
   *nchunks = cp.nchunks;
   return 1;
 }
+
+int hg_set_chunking(int enable) { return hg::g_chunking.exchange(enable ? 1 : 0); }
 
 int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout) {
   return host_product(Kind::Ntt, x, nx, y, ny, 0, out, nout);

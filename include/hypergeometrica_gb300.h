@@ -81,6 +81,13 @@ size_t hg_ntt_length(size_t nx, size_t ny);
 // arithmetic only: needs no device and no hg_init.
 int hg_chunk_plan(size_t nx, size_t ny, int *log_len, size_t *chunk, size_t *nchunks);
 
+// Whether unbalanced products may run in chunks (hg_chunk_plan); on by
+// default.  With 0 every product runs as the reference's one transform of
+// hg_ntt_length(nx, ny) points.  Returns the previous setting.  Process-wide;
+// takes effect for products enqueued after it returns.  No counterpart in
+// the reference.
+int hg_set_chunking(int enable);
+
 /* ---- products on host memory ------------------------------------------ */
 
 // mpz-*/ntt (src/ntt-multiply.lisp:174-254): |x| * |y| through the three-prime

@@ -65,6 +65,13 @@ def test_chunk_plan_invariants(lib):
             assert L < (nl + ns - 1).bit_length(), plan
             seen.add(L)
     assert any(L <= 12 for L in seen) and any(L > 12 for L in seen)
+    # With chunking off every product runs as one transform.
+    assert _lib.set_chunking(False) is True
+    try:
+        assert _lib.chunk_plan(1 << 24, 1 << 16) is None
+    finally:
+        assert _lib.set_chunking(True) is False
+    assert _lib.chunk_plan(1 << 24, 1 << 16) is not None
 
 
 def test_no_cpu_fallback_without_gpu(lib):

@@ -72,6 +72,7 @@ def test_chunked_equals_single_transform(hg):
     """The chunked device product equals the batch path's single transform."""
     import torch
 
+    from hypergeometrica_gb300 import _lib
     from hypergeometrica_gb300 import device as D
 
     for nx, ny in ((1 << 22, 1 << 12), (1 << 21, 77777), (5 << 18, 1 << 17)):
@@ -88,6 +89,14 @@ def test_chunked_equals_single_transform(hg):
         D.mul(ty, tx, c)        # operands swapped
         D.sync()
         assert torch.equal(c, a[: nx + ny]), (nx, ny)
+        d = torch.full((nx + ny,), -1, dtype=torch.int64, device="cuda")
+        _lib.set_chunking(False)
+        try:
+            D.mul(tx, ty, d)    # the reference's one transform through hg_mul_device
+            D.sync()
+        finally:
+            _lib.set_chunking(True)
+        assert torch.equal(d, a[: nx + ny]), (nx, ny)
 
 
 def test_chunked_host_paths(hg, oracle):
