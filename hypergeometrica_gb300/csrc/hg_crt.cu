@@ -73,6 +73,8 @@ struct CrtProducer {
     }
   }
 
+  // Residues may be any 64-bit values congruent to the coefficient (the
+  // inverse leaves [0, 2p)): every one enters through a Shoup product.
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
@@ -100,16 +102,21 @@ struct CrtProducer {
 // 2^(logN-1) makes at most two chunks meet at a position.  Their residues
 // are added before the reconstruction: the sum of the two coefficients is
 // below 2 * short * 2^128, far below p0 p1 p2, so Garner's value of the
-// summed residues is the exact sum.
+// summed residues is the exact sum.  The inverse leaves residues in
+// [0, 2p); each is folded to [0, p) before the sum, and Garner's Shoup
+// products take the sum in [0, 2p) as it is.
 struct ChunkProducer {
   CrtProducer crt;      // res = chunk 0's residues, n = 2^logN
   uint64_t stride;      // words between consecutive chunks' residues
   uint64_t chunk, nchunks;
 
+  __device__ __forceinline__ static uint64_t sum2(uint64_t a, uint64_t b, uint64_t p) {
+    return (a >= p ? a - p : a) + (b >= p ? b - p : b);
+  }
+
   __device__ __forceinline__ uint64_t sum_res(const uint64_t *r0, const uint64_t *r1, int j) const {
-    const uint64_t p = crt.k.pc[j].p;
     const uint64_t a = r0 ? r0[j * crt.n] : 0, b = r1 ? r1[j * crt.n] : 0;
-    return add_mod(a, b, p);
+    return sum2(a, b, crt.k.pc[j].p);
   }
 
   // Residue pointers of position i: the chunk that starts at or below i, and
@@ -144,8 +151,8 @@ struct ChunkProducer {
         ulonglong2 a = make_ulonglong2(0, 0), b = make_ulonglong2(0, 0);
         if (r0) a = __ldg(reinterpret_cast<const ulonglong2 *>(r0 + j * crt.n) + q);
         if (r1) b = __ldg(reinterpret_cast<const ulonglong2 *>(r1 + j * crt.n) + q);
-        r[j][2 * q] = add_mod(a.x, b.x, p);
-        r[j][2 * q + 1] = add_mod(a.y, b.y, p);
+        r[j][2 * q] = sum2(a.x, b.x, p);
+        r[j][2 * q + 1] = sum2(a.y, b.y, p);
       }
     }
 #pragma unroll

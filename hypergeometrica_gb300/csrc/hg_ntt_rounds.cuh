@@ -62,6 +62,13 @@ __device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const ui
 // the thread's row bits below b (runtime, zero when TZERO) and the register's
 // (compile time).  With TZERO, butterflies whose twiddle is 1 skip the
 // multiplication.
+//
+// Forward (DIF) butterflies keep every residue in [0, p), as ntt-forward
+// does.  Inverse (DIT) butterflies take and leave [0, 2p) (2p < 2^64): u is
+// folded once, v w is a corrected Shoup product (v folded when w = 1), and
+// u + t, u - t + p need no correction.  Every consumer of an inverse
+// residue accepts [0, 2p): the next pass's Montgomery pre-twiddle, the 1/N
+// scaling and the reconstruction's Shoup products.
 template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO>
 __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__restrict__ tw, uint32_t xt, uint64_t p,
                                        uint32_t c) {
@@ -88,13 +95,16 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__re
           v[i | (1 << j)] = shoup_mul(u - w + p, t.x, t.y, p, c);  // u - w + p in (0, 2p)
         }
       } else {
-        uint64_t t = w;
-        if (!trivial) {
+        const uint64_t uu = u >= p ? u - p : u;
+        uint64_t t;
+        if (trivial) {
+          t = w >= p ? w - p : w;
+        } else {
           const ulonglong2 tt = tw[ts ^ swz_tw(rp << sh)];
           t = shoup_mul(w, tt.x, tt.y, p, c);
         }
-        v[i] = add_mod(u, t, p);
-        v[i | (1 << j)] = sub_mod(u, t, p);
+        v[i] = uu + t;               // [0, 2p)
+        v[i | (1 << j)] = uu - t + p;  // (0, 2p)
       }
     }
   }

@@ -3,11 +3,12 @@
 // The NTT passes are bound by the integer pipes, not by HBM: each radix-2
 // butterfly is a 64-bit modular add, a subtract and a Shoup product built
 // from 32-bit IMAD and ALU instructions.  This kernel runs the same
-// butterflies (hg_common.cuh's add_mod / sub_mod / shoup_mul) on 16
-// registers per thread with twiddles from shared memory and no global
-// traffic, half forward (DIF) and half inverse (DIT), over every SM: its
-// rate is the practical peak a memory-free butterfly network reaches on this
-// GPU, the denominator of the product's integer-pipe roofline.
+// butterflies (hg_ntt_rounds.cuh's stages: canonical forward, inverse on
+// [0, 2p)) on 16 registers per thread with twiddles from shared memory and
+// no global traffic, half forward (DIF) then half inverse (DIT), over every
+// SM: its rate is the practical peak a memory-free butterfly network
+// reaches on this GPU, the denominator of the product's integer-pipe
+// roofline.
 #include <cstdio>
 
 #include "hg_host.h"
@@ -30,7 +31,7 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
   for (int i = 0; i < 16; ++i) v[i] = (gid * 16 + i) % p;
   const int off = threadIdx.x & 7;
   for (int it = 0; it < kPeakIters; ++it) {
-    const bool dit = it & 1;
+    const bool dit = it >= kPeakIters / 2;
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
 #pragma unroll
@@ -42,9 +43,10 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
           v[i] = add_mod(u, x, p);
           v[i | (1 << j)] = shoup_mul(u - x + p, t.x, t.y, p, c);
         } else {
+          const uint64_t uu = u >= p ? u - p : u;
           const uint64_t y = shoup_mul(x, t.x, t.y, p, c);
-          v[i] = add_mod(u, y, p);
-          v[i | (1 << j)] = sub_mod(u, y, p);
+          v[i] = uu + y;
+          v[i | (1 << j)] = uu - y + p;
         }
       }
     }
