@@ -44,14 +44,14 @@ struct Groups {
   __host__ __device__ static constexpr int JG() { return 4 - NB<g>(); }
 };
 
-template <int T, int g, bool INV>
+template <int T, int g, bool INV, bool EDGE = false>
 __device__ __forceinline__ void round_g(uint64_t (&v)[16], const ulonglong2 *tw, uint32_t xt, uint64_t p, uint32_t c) {
   using Gr = Groups<T>;
   constexpr int A = Gr::template A<g>();
   constexpr int NB = Gr::template NB<g>();
   constexpr int JG = Gr::template JG<g>();
   constexpr bool TZERO = (g == 0) && (A == 0) && (JG == 0);
-  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO>(v, tw, xt, p, c);
+  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO, EDGE && TZERO>(v, tw, xt, p, c);
 }
 
 // Move the thread's registers from the layout of group g to that of group h
@@ -88,12 +88,13 @@ __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, 
   }
 }
 
-// All inverse rounds, from group 0 up to the top group.
-template <int T>
+// All inverse rounds, from group 0 up to the top group.  CANON_IN: the
+// residues come from the pointwise product, in [0, p).
+template <int T, bool CANON_IN = false>
 __device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
-  round_g<T, 0, true>(v, tw, xt, p, c);
+  round_g<T, 0, true, CANON_IN>(v, tw, xt, p, c);
   if constexpr (G >= 2) {
     regroup<T, 0, 1>(v, sm, xt, tid);
     round_g<T, 1, true>(v, tw, xt, p, c);
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(spec + (xt | (static_cast<uint32_t>(i) << A0))), p, c);
     }
-    inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
+    inverse_rounds<T, true>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
     if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     return;
   } else {
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig
         for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
       }
       // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
-      inverse_rounds<T>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
+      inverse_rounds<T, true>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
       if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
     }
   }

@@ -69,9 +69,15 @@ __device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const ui
 // u + t, u - t + p need no correction.  Every consumer of an inverse
 // residue accepts [0, 2p): the next pass's Montgomery pre-twiddle, the 1/N
 // scaling and the reconstruction's Shoup products.
-template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO>
+//
+// EDGE marks the stage on row bit 0 (BLO = 0, twiddle 1) of a pass whose
+// neighbour is a Montgomery product: forward, it is the last stage and its
+// u + v, u - v + p go uncorrected ([0, 2p)) into the inter-pass twiddle;
+// inverse, it is the first stage and its inputs are already in [0, p).
+template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO, bool EDGE = false>
 __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__restrict__ tw, uint32_t xt, uint64_t p,
                                        uint32_t c) {
+  static_assert(!EDGE || (TZERO && BLO == 0), "the edge stage is the twiddle-free stage on row bit 0");
 #pragma unroll
   for (int s = 0; s < NB; ++s) {
     const int jj = INV ? s : NB - 1 - s;
@@ -86,6 +92,11 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__re
       const uint32_t rp = ((static_cast<uint32_t>(i) << A) >> ROWOFF) & lowmask;
       const bool trivial = TZERO && rp == 0;
       const uint64_t u = v[i], w = v[i | (1 << j)];
+      if (EDGE && jj == 0) {  // twiddle 1, inputs in [0, p): outputs in [0, 2p)
+        v[i] = u + w;
+        v[i | (1 << j)] = u - w + p;
+        continue;
+      }
       if (!INV) {
         v[i] = add_mod(u, w, p);
         if (trivial) {

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
       xt = thread_base<A0>(tid);
       from_smem<A0>(v, sm, xt);
     }
-    stages<4, 0, A0, ROWOFF, 0, LOGR, false, true>(v, tw, xt, p, c);
+    stages<4, 0, A0, ROWOFF, 0, LOGR, false, true, true>(v, tw, xt, p, c);  // then the inter-pass twiddle
     inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
     offsets(xt, A0, off, step);
 #pragma unroll
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
     for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
     inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
     __syncthreads();  // twiddle table ready
-    stages<4, 0, A0, ROWOFF, 0, LOGR, true, true>(v, tw, xt, p, c);
+    stages<4, 0, A0, ROWOFF, 0, LOGR, true, true, true>(v, tw, xt, p, c);  // after the inter-pass twiddle
     if constexpr (G == 2) {
       to_smem<A0>(sm, v, xt);
       __syncthreads();
