@@ -19,7 +19,8 @@
 namespace hg {
 namespace {
 
-constexpr int kCarryThreads = 256;
+constexpr int kCarryThreads = 512;
+constexpr int kCarryMinBlocks = 2;  // 64 registers
 constexpr int kCarryPer = 8;
 constexpr int kCarryTile = kCarryThreads * kCarryPer;
 constexpr int kSpinLimit = 1 << 22;
@@ -257,13 +258,15 @@ __device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, uint64_t 
   }
 }
 
-// One tile of 2048 output limbs per CTA.  Single product: tiles in ticket
+// One tile of 4096 output limbs per CTA.  Single product: tiles in ticket
 // order.  Batch (batch != nullptr): tickets run product-major, tpp tiles per
 // product; product k's residues are rebased by k * ws_stride, its output is
 // batch[k].out[0, min(nout, n)), and the look-back stops at its first tile.
-// Four CTAs per SM (64 registers): slightly faster than three.
+// Tiles of 4096 limbs, two 512-thread CTAs per SM (64 registers): 4% faster
+// than 2048-limb tiles at four CTAs per SM, with half as many tiles in
+// flight for the look-back to cross.
 template <class Producer>
-__global__ void __launch_bounds__(kCarryThreads, 4) carry_kernel(const Producer prod0, uint64_t *__restrict__ out,
+__global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(const Producer prod0, uint64_t *__restrict__ out,
                                                               uint64_t nproc, ScanState ss, const ProductDesc *batch,
                                                               uint64_t tpp, uint64_t ws_stride, uint64_t n) {
   __shared__ uint64_t s_prev[kCarryThreads][9];

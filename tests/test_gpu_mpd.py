@@ -7,13 +7,23 @@ result is checked against an independent pi to 2^-b.  The truncated variant
 is not the reference's mantissa; it must agree with pi/10 to the bits asked.
 """
 
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 
 import mpd_oracle as M
 import series_oracle as O
+from conftest import ROOT
 
 pytestmark = pytest.mark.gpu
+
+
+def _mpd_pi_fixtures():
+    with open(os.path.join(ROOT, "tests", "golden", "mpd_pi.json")) as f:
+        return json.load(f)["fixtures"]
 
 
 def _pair(x):
@@ -27,6 +37,22 @@ def test_mpd_pi_bit_identical(hg, bits):
     got = G.mpd_pi(bits)
     want = M.mpd_pi(bits)
     assert _pair(got) == (want.m, want.e)
+
+
+@pytest.mark.parametrize("fx", _mpd_pi_fixtures(), ids=lambda f: f"{f['bits']}bits")
+def test_mpd_pi_bit_identical_golden(hg, fx):
+    """Untruncated mpd-pi at up to 2^18 bits against the oracle's result
+    (tests/golden/make_mpd_pi_golden.py): exponent, sign, length, end limbs
+    and SHA-256 of the mantissa's little-endian limbs."""
+    from hypergeometrica_gb300 import mpd as G
+
+    got = G.mpd_pi(fx["bits"])
+    mant = got.mantissa
+    limbs = np.trim_zeros(mant.t[: mant.size].cpu().numpy().view(np.uint64), "b")
+    assert got.exponent == fx["exponent"]
+    assert mant.sign == fx["sign"] and limbs.size == fx["limbs"]
+    assert hex(int(limbs[0])) == fx["low_limb"] and hex(int(limbs[-1])) == fx["high_limb"]
+    assert hashlib.sha256(limbs.tobytes()).hexdigest() == fx["sha256"]
 
 
 def test_reciprocal_and_inv_sqrt_bit_identical(hg):
