@@ -737,7 +737,7 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
 //
 // Scratch layout, in words: operand 0's residues [3][2^16], operand 1's
 // residues [3][2^16], the carry scan's ticket word, then one flag word per
-// carry tile (32 at 2^16).  Static device memory is zero when the module
+// carry tile (16 at 2^16).  Static device memory is zero when the module
 // loads; the residue area needs no initial value (the first pass writes
 // every word it later reads), and the call clears the ticket and flag words
 // on its stream before each reconstruction.
