@@ -103,6 +103,7 @@ SIGNATURES = {
     "hg_trim_batch_device": (ctypes.c_int, [_vp, _sz, _vp, _vp]),
     "hg_mul_small_batch_device": (ctypes.c_int, [_vp, _sz, _vp]),
     "hg_series_leaves_device": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp]),
+    "hg_series_nodes_device": (ctypes.c_int, [_vp, _vp, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp, _vp]),
     "hg_butterfly_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "hg_svc_open": (ctypes.c_int, [_sz, ctypes.c_int, _sz, ctypes.POINTER(_vp)]),
     "hg_svc_submit": (ctypes.c_int, [_vp, ctypes.POINTER(HgProduct), _sz, ctypes.POINTER(ctypes.c_uint64)]),

@@ -33,7 +33,7 @@ from typing import Callable
 
 import numpy as np
 
-from ._lib import check, load
+from ._lib import HGError, check, load
 from .mpz import NTT_MULTIPLY_THRESHOLD, digits_from_int, int_from_digits
 
 
@@ -192,6 +192,10 @@ def trim_sizes(vecs) -> np.ndarray:
 
 
 SMALL_MAX_LIMBS = 64  # HG_SMALL_MAX_LIMBS
+# Tree nodes of height <= NODE_HEIGHT (at most 2^NODE_HEIGHT terms) whose
+# parent is higher are computed whole on the device (hg_series_nodes_device)
+# instead of level by level.
+NODE_HEIGHT = 6
 
 
 def _multiply_records(rec: np.ndarray, service) -> None:
@@ -242,17 +246,18 @@ def _sum_records(rec: np.ndarray) -> np.ndarray:
 # ---- the recursion tree -------------------------------------------------
 
 
-def _tree(lower: int, upper: int):
-    """The nodes of binary-split's recursion over [lower, upper), top down:
-    arrays lo, hi, left child, right child (-1 for leaves), height
-    (= ceil(log2(hi - lo)) for this split)."""
+def _tree(lower: int, upper: int, stop: int = 1):
+    """The nodes of binary-split's recursion over [lower, upper), top down,
+    not expanding nodes of at most `stop` terms: arrays lo, hi, left child,
+    right child (-1 for unexpanded nodes), height (= ceil(log2(hi - lo)) for
+    this split)."""
     lo = [np.array([lower], dtype=np.int64)]
     hi = [np.array([upper], dtype=np.int64)]
     first = [0]
     lefts, rights = [], []
     cur_lo, cur_hi, nid = lo[0], hi[0], 1
     while True:
-        inner = (cur_hi - cur_lo) > 1
+        inner = (cur_hi - cur_lo) > stop
         left = np.full(cur_lo.size, -1, dtype=np.int64)
         right = np.full(cur_lo.size, -1, dtype=np.int64)
         k = int(inner.sum())
@@ -312,7 +317,9 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
     if upper <= lower:
         raise ValueError("binary-split needs upper > lower")
     t_start = time.perf_counter()
-    lo, hi, left, right, height = _tree(lower, upper)
+    whole = _device_leaves_fit(series, upper)
+    # Whole nodes: the tree stops at nodes of at most 2^NODE_HEIGHT terms.
+    lo, hi, left, right, height = _tree(lower, upper, (1 << NODE_HEIGHT) if whole else 1)
     nn = lo.size
     if timings is not None:
         timings.append(("tree", int(nn), time.perf_counter() - t_start))
@@ -321,18 +328,32 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
     ptr = np.zeros((4, nn), dtype=np.uint64)
     size = np.zeros((4, nn), dtype=np.int64)
     sign = np.ones((4, nn), dtype=np.int64)
-    # binary-split-base-case=1 (:102-110): P = p(k), Q = q(k), B = b(k), R = p(k) a(k)
-    if _device_leaves_fit(series, upper):
-        arena0, ss = _device_leaves(series, lower, upper)
+    H = int(height.max())
+    h_first, arena_key = 1, 0  # the first height combined level by level; key of the base arena
+    root_off = None  # the root's arena and the offsets of its P, Q, B, R
+    if whole:
+        # The unexpanded nodes (height <= h0, parent higher): one device
+        # thread each folds the node's terms (the same integers as the
+        # reference's recursion below that node).  Their parents are at
+        # heights h0 + 1 and h0 + 2.
+        h0 = NODE_HEIGHT
+        cut = leaves
+        arena0, ss, width = _device_nodes(series, lo[cut], hi[cut], upper)
         base = arena0.data_ptr()
-        count = upper - lower
-        kidx = (lo[leaves] - lower).astype(np.uint64)
+        nc = np.uint64(cut.size)
+        cidx = np.arange(cut.size, dtype=np.uint64)
         for j in range(4):
-            ptr[j, leaves] = base + 8 * 4 * (np.uint64(j * count) + kidx)
-            sign[j, leaves] = ss[j, kidx, 0]
-            size[j, leaves] = ss[j, kidx, 1]
-        leaf_limbs = int(size[:, leaves].sum())
+            ptr[j, cut] = base + np.uint64(8 * width) * (np.uint64(j) * nc + cidx)
+            sign[j, cut] = ss[j, :, 0]
+            size[j, cut] = ss[j, :, 1]
+        if (size[:, cut] < 0).any():
+            raise HGError(-1, "series node partial exceeded its width bound")
+        leaf_limbs = int(size[:, cut].sum())
+        h_first, arena_key = h0 + 1, h0
+        if cut[0] == 0:  # the root itself
+            root_off = (arena0, [j * cut.size * width for j in range(4)])
     else:
+        # binary-split-base-case=1 (:102-110): P = p(k), Q = q(k), B = b(k), R = p(k) a(k)
         ks = lo[leaves].tolist()
         pv = [series.p(k) for k in ks]
         vals = [pv, [series.q(k) for k in ks], [series.b(k) for k in ks],
@@ -347,10 +368,10 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
             size[j, leaves] = sz
             sign[j, leaves] = sg
             base_off += w * leaves.size
-    root_off = None  # the root's arena and the offsets of its P, Q, B, R
-    arenas = {0: arena0}
+        if H == 0:
+            root_off = (arena0, [int((ptr[j, 0] - np.uint64(base)) // np.uint64(8)) for j in range(4)])
+    arenas = {arena_key: arena0}
     del arena0
-    H = int(height.max())
     if timings is not None:
         timings.append(("leaves", int(leaves.size), time.perf_counter() - t_start))
     own = []
@@ -369,7 +390,7 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
     try:
         order = np.argsort(height, kind="stable")
         bounds = np.searchsorted(height[order], np.arange(H + 2))
-        for h in range(1, H + 1):
+        for h in range(h_first, H + 1):
             idx = order[bounds[h]: bounds[h + 1]]
             L, R = left[idx], right[idx]
             k = idx.size
@@ -428,12 +449,8 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
             svc.close()
 
     def dev_int(j: int) -> DeviceInt:
-        if H == 0:
-            t = arenas[0][int((ptr[j, 0] - np.uint64(base)) // np.uint64(8)):]
-        else:
-            arena, o = root_off
-            t = arena[o[j]:]
-        return DeviceInt(int(sign[j, 0]), t, int(size[j, 0]))
+        arena, o = root_off
+        return DeviceInt(int(sign[j, 0]), arena[o[j]:], int(size[j, 0]))
 
     return Partial(lower, upper, dev_int(0), dev_int(1), dev_int(2), dev_int(3))
 
@@ -442,6 +459,41 @@ def _device_leaves(series: Series, lower: int, upper: int):
     """hg_series_leaves_device: ((4 * count * 4) limb arena, (4, count, 2) signs and sizes)."""
     import torch
 
+    count = upper - lower
+    limbs = torch.empty(16 * count, dtype=torch.int64, device="cuda")
+    ss = torch.empty(8 * count, dtype=torch.int64, device="cuda")
+    st = torch.cuda.current_stream()
+    check(load().hg_series_leaves_device(_polys(series), lower, count, limbs.data_ptr(), ss.data_ptr(),
+                                         st.cuda_stream))
+    return limbs, ss.cpu().numpy().reshape(4, count, 2)
+
+
+def _device_nodes(series: Series, lo: np.ndarray, hi: np.ndarray, upper: int):
+    """hg_series_nodes_device for the node ranges [lo, hi): ((4 * n * width)
+    limb arena, (4, n, 2) signs and sizes, width).  The width bounds every
+    value: with s_v the limbs of the largest |v(k)|, k < upper, and
+    S = s_p + s_q + s_b + s_r + 1, a node of m terms has |R| < 2^(64 m S)
+    and P, Q, B, B P below that."""
+    import torch
+
+    n = int(lo.size)
+    bits = [_poly_bits(spec, max(1, upper - 1)) for spec in series.poly]  # a, b, p, q
+    lim = lambda b: max(1, -(-b // 64))  # noqa: E731
+    S = lim(bits[2]) + lim(bits[3]) + lim(bits[1]) + lim(bits[2] + bits[0]) + 1
+    width = max(8, S * int((hi - lo).max()) + 1)
+    ranges = torch.from_numpy(np.stack([lo, hi], axis=1).reshape(-1).astype(np.int64)).cuda()
+    limbs = torch.empty(4 * n * width, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(2 * n * width, dtype=torch.int64, device="cuda")
+    ss = torch.empty(8 * n, dtype=torch.int64, device="cuda")
+    st = torch.cuda.current_stream()
+    check(load().hg_series_nodes_device(_polys(series), ranges.data_ptr(), n, width, limbs.data_ptr(),
+                                        ss.data_ptr(), scratch.data_ptr(), st.cuda_stream))
+    out = ss.cpu().numpy().reshape(4, n, 2)
+    del scratch, ranges
+    return limbs, out, width
+
+
+def _polys(series: Series):
     from ._lib import HgPoly
 
     polys = (HgPoly * 4)()
@@ -451,12 +503,7 @@ def _device_leaves(series: Series, lower: int, upper: int):
         polys[j].degree = len(coefs) - 1
         polys[j].has_zero_value = 0 if zero is None else 1
         polys[j].zero_value = 0 if zero is None else zero
-    count = upper - lower
-    limbs = torch.empty(16 * count, dtype=torch.int64, device="cuda")
-    ss = torch.empty(8 * count, dtype=torch.int64, device="cuda")
-    st = torch.cuda.current_stream()
-    check(load().hg_series_leaves_device(polys, lower, count, limbs.data_ptr(), ss.data_ptr(), st.cuda_stream))
-    return limbs, ss.cpu().numpy().reshape(4, count, 2)
+    return polys
 
 
 def _offsets(sizes_list):

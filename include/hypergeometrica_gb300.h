@@ -262,6 +262,19 @@ typedef struct hg_poly {
 int hg_series_leaves_device(const hg_poly *polys, uint64_t lower, uint64_t count, uint64_t *limbs,
                             int64_t *sign_size, void *stream);
 
+/* binary-split (src/binary-splitting.lisp:112-133) of whole nodes: the
+ * partial P, Q, B, R over terms [ranges[2 i], ranges[2 i + 1]) for each of
+ * the n nodes, one device thread per node folding its terms left to right
+ * (a range's partial is the same integers however the range is split).
+ * Value j of node i goes to limbs[(j n + i) width ..] (magnitude) and
+ * sign_size[(j n + i) 2] = sign (+1 for zero), [.. + 1] = length without
+ * high zero limbs, or -1 when a value would need more than width limbs.
+ * scratch holds 2 n width words.  All arrays are device memory.  Every
+ * term's values and p(k) a(k) must fit in 255 bits, as for
+ * hg_series_leaves_device. */
+int hg_series_nodes_device(const hg_poly *polys, const uint64_t *ranges, uint64_t n, uint64_t width,
+                           uint64_t *limbs, int64_t *sign_size, uint64_t *scratch, void *stream);
+
 /* ---- device-resident multiply service ---------------------------------- */
 
 /* Replaces the one-product-at-a-time mpz-* calls that binary-split / combine

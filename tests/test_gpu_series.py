@@ -166,6 +166,70 @@ def test_device_leaves_match_python(hg, name, lo, count):
             assert _as_int(host[j, i]) == abs(v), (j, k)
 
 
+@pytest.mark.parametrize("name", sorted(SERIES) + ["exp"])
+def test_device_nodes_match_oracle(hg, name):
+    """hg_series_nodes_device: whole-node partials (one thread folding each
+    range) equal the oracle's binary-split of the same ranges."""
+    from hypergeometrica_gb300 import series as S
+
+    if name == "exp":
+        ser, oser = S.make_exp_series("-5/3"), O.exp_series("-5/3")
+    else:
+        ser, oser = getattr(S, SERIES[name][0])(), SERIES[name][1]
+    ranges = [(0, 1), (0, 2), (1, 2), (0, 32), (7, 30), (1000, 1031), (10**6, 10**6 + 17),
+              ((1 << 31) - 40, (1 << 31) - 8)]
+    lo = np.array([r[0] for r in ranges], dtype=np.int64)
+    hi = np.array([r[1] for r in ranges], dtype=np.int64)
+    upper = int(hi.max())
+    assert S._device_leaves_fit(ser, upper)
+    limbs, ss, width = S._device_nodes(ser, lo, hi, upper)
+    host = limbs.cpu().numpy().view(np.uint64).reshape(4, len(ranges), width)
+    for i, (a, b) in enumerate(ranges):
+        want = O.binary_split(oser, a, b)
+        for j, v in enumerate(want):
+            size = (abs(v).bit_length() + 63) // 64
+            assert ss[j, i, 1] == size, (name, a, b, j)
+            assert ss[j, i, 0] == (-1 if v < 0 else 1), (name, a, b, j)
+            assert _as_int(host[j, i, :size]) == abs(v), (name, a, b, j)
+
+
+def test_device_nodes_width_bound(hg):
+    """A width too small for a node's values is reported as size -1; the
+    kernel writes nothing past the width (checked before every write)."""
+    import torch
+
+    from hypergeometrica_gb300 import series as S
+    from hypergeometrica_gb300._lib import load
+
+    ser = S.make_chudnovsky_series()
+    n, width = 2, 8
+    ranges = torch.tensor([0, 1, 0, 30], dtype=torch.int64, device="cuda")
+    limbs = torch.full((4 * n * width + 64,), -7, dtype=torch.int64, device="cuda")
+    scratch = torch.full((2 * n * width + 64,), -7, dtype=torch.int64, device="cuda")
+    ss = torch.empty(8 * n, dtype=torch.int64, device="cuda")
+    st = torch.cuda.current_stream()
+    assert load().hg_series_nodes_device(S._polys(ser), ranges.data_ptr(), n, width, limbs.data_ptr(),
+                                         ss.data_ptr(), scratch.data_ptr(), st.cuda_stream) == 0
+    out = ss.cpu().numpy().reshape(4, n, 2)
+    assert (out[:, 0, 1] >= 0).all()  # one term fits
+    assert (out[:, 1, 1] == -1).all()  # thirty terms do not
+    assert (limbs[4 * n * width:] == -7).all() and (scratch[2 * n * width:] == -7).all()
+
+
+@pytest.mark.parametrize("node_height", [0, 2, 3, 7])
+def test_binary_split_node_heights(hg, monkeypatch, node_height):
+    """The split's result does not depend on where the tree is cut into
+    whole nodes."""
+    from hypergeometrica_gb300 import series as S
+
+    monkeypatch.setattr(S, "NODE_HEIGHT", node_height)
+    for maker, oser, lo, hi in (("make_chudnovsky_series", O.chudnovsky_series(), 0, 700),
+                                ("make_apery_series", O.apery_series(), 3, 260)):
+        part = S.binary_split(getattr(S, maker)(), lo, hi)
+        want = O.binary_split(oser, lo, hi)
+        assert (part.p.to_int(), part.q.to_int(), part.b.to_int(), part.r.to_int()) == want
+
+
 def test_python_leaves_for_a_series_without_polynomials(hg):
     from hypergeometrica_gb300 import series as S
 
