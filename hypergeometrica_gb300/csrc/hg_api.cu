@@ -129,7 +129,7 @@ struct Context {
   DevBuf tables;
   cudaStream_t stream = nullptr;
   DevBuf A, B, X, Y, OUT, flags;
-  DevBuf misc;  // [0] ticket (u64), [1] error word (int)
+  DevBuf misc;  // bytes [0, 8) carry-scan ticket, [8, 12) error word, [16, 24) large-sum top index
   unsigned long long ticket_count = 0;
   uint32_t epoch = 0;
   cudaEvent_t ws_done = nullptr;
@@ -1283,6 +1283,27 @@ int enqueue_batch(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) {
 
 std::recursive_mutex &lib_mutex() { return g_ctx.mu; }
 bool lib_ready() { return g_ctx.ready; }
+int large_sum_device(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
+                     uint64_t *out, uint64_t nout, int64_t *result, cudaStream_t st) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  const uint64_t n = na > nb ? na : nb;
+  const uint64_t nproc = sa != sb ? n : n + 1;
+  HG_CUDA(ws_acquire(st), "workspace ordering");
+  if (nout > nproc) HG_CUDA(cudaMemsetAsync(out + nproc, 0, (nout - nproc) * sizeof(uint64_t), st), "zero tail");
+  ScanState ss;
+  rc = scan_state(carry_tiles(nproc), &ss);
+  if (rc) return rc;
+  long long *top = reinterpret_cast<long long *>(static_cast<char *>(g_ctx.misc.p) + 16);
+  {
+    ProfScope ps(HG_KC_OTHER, st, 24.0 * static_cast<double>(nproc));
+    HG_CUDA(launch_large_sum(a, na, sa, b, nb, sb, out, top, result, ss, st), "large sum");
+  }
+  HG_CUDA(ws_release(st), "workspace ordering");
+  return HG_OK;
+}
+
 int lib_device() { return g_ctx.device; }
 
 int lib_fail(int code, const char *fmt, ...) {

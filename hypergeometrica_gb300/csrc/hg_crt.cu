@@ -74,6 +74,8 @@ struct CrtProducer {
     }
   }
 
+  __device__ __forceinline__ bool drop_top() const { return false; }
+
   // Residues may be any 64-bit values congruent to the coefficient (the
   // inverse leaves [0, 2p)): every one enters through a Shoup product.
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
@@ -110,6 +112,8 @@ struct ChunkProducer {
   CrtProducer crt;      // res = chunk 0's residues, n = 2^logN
   uint64_t stride;      // words between consecutive chunks' residues
   uint64_t chunk, nchunks;
+
+  __device__ __forceinline__ bool drop_top() const { return false; }
 
   __device__ __forceinline__ static uint64_t sum2(uint64_t a, uint64_t b, uint64_t p) {
     return (a >= p ? a - p : a) + (b >= p ? b - p : b);
@@ -168,6 +172,8 @@ struct ConvProducer {
   uint64_t ny;
   uint64_t dval;
 
+  __device__ __forceinline__ bool drop_top() const { return false; }
+
   __device__ __forceinline__ void eight(uint64_t, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
 #pragma unroll
     for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? at(0, i0 + k8) : V3{0, 0, 0};
@@ -192,6 +198,94 @@ struct ConvProducer {
     return v;
   }
 };
+
+// mpz-+ of two long magnitudes over the whole GPU (%add-storages/unsafe and
+// %subtract-storages/unsafe, src/mpz-ram.lisp:184-274): position i holds
+// x_i + y_i as (low, carry).  With opposite signs y is the smaller
+// magnitude's complement over n = max(na, nb) limbs plus 1 at position 0,
+// and the carry out of the top is dropped.  `top` is then the highest index
+// where a and b differ (or -1), found before the scan; it picks the larger.
+struct SumProducer {
+  const uint64_t *a, *b;
+  uint64_t na, nb, n;
+  const long long *top;  // subtraction only
+
+  __device__ __forceinline__ bool drop_top() const { return top != nullptr; }
+
+  __device__ __forceinline__ bool a_larger() const {
+    if (!top) return true;
+    const long long t = *top;
+    if (t < 0) return true;
+    const uint64_t u = static_cast<uint64_t>(t);
+    return (u < na ? a[u] : 0) >= (u < nb ? b[u] : 0);
+  }
+
+  __device__ __forceinline__ V3 value(uint64_t i, bool ax) const {
+    if (i >= n) return V3{0, 0, 0};
+    const uint64_t *X = ax ? a : b, *Y = ax ? b : a;
+    const uint64_t nX = ax ? na : nb, nY = ax ? nb : na;
+    const uint64_t x = i < nX ? X[i] : 0;
+    uint64_t y = i < nY ? Y[i] : 0;
+    if (top) y = ~y;
+    uint64_t lo = x + y;
+    uint64_t c = lo < x ? 1 : 0;
+    if (top && i == 0) {
+      lo += 1;
+      c += lo == 0 ? 1 : 0;
+    }
+    return V3{lo, c, 0};
+  }
+
+  __device__ __forceinline__ void prefetch(uint64_t, uint64_t, uint64_t) const {}
+
+  __device__ __forceinline__ V3 at(uint64_t, uint64_t i) const { return value(i, a_larger()); }
+
+  __device__ __forceinline__ void eight(uint64_t, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
+    const bool ax = a_larger();
+#pragma unroll
+    for (int k8 = 0; k8 < 8; ++k8) v[k8] = (i0 + k8 < nproc) ? value(i0 + k8, ax) : V3{0, 0, 0};
+  }
+};
+
+// *top = max index i < n with a_i != b_i (the caller set it to -1).
+__global__ void top_diff_kernel(const uint64_t *a, uint64_t na, const uint64_t *b, uint64_t nb, uint64_t n,
+                                long long *top) {
+  long long best = -1;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    if ((i < na ? a[i] : 0) != (i < nb ? b[i] : 0)) best = static_cast<long long>(i);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const long long o = __shfl_down_sync(0xffffffffu, best, d);
+    best = o > best ? o : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best >= 0) atomicMax(top, best);
+}
+
+// result = (sign, size) of out[0, nproc): the highest nonzero limb, scanned
+// from the top 2048 limbs at a time by one CTA.
+__global__ void sum_finish_kernel(const uint64_t *out, uint64_t nproc, SumProducer prod, int64_t sa, int64_t sb,
+                                  int64_t *result) {
+  __shared__ long long s_top;
+  if (threadIdx.x == 0) s_top = -1;
+  __syncthreads();
+  for (uint64_t hi = nproc; hi > 0;) {
+    const uint64_t lo = hi > 2048 ? hi - 2048 : 0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+      if (out[i]) atomicMax(&s_top, static_cast<long long>(i));
+    __syncthreads();
+    const bool found = s_top >= 0;  // read by all before any update for the next chunk
+    __syncthreads();
+    if (found) break;
+    hi = lo;
+  }
+  if (threadIdx.x == 0) {
+    const int64_t size = s_top + 1;
+    const int64_t sign = prod.a_larger() ? sa : sb;
+    result[0] = size ? sign : 1;
+    result[1] = size;
+  }
+}
 
 __device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t state, uint32_t g, uint32_t p) {
   return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | state;
@@ -375,7 +469,8 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
       reinterpret_cast<volatile unsigned long long *>(ss.flags)[gt] = flag_word(ss.epoch, 2, cout, 0);
       s_cin = cin;
       const uint64_t last = tile * kCarryTile + kCarryTile;
-      if (last >= nproc && tile * kCarryTile < nproc && cout) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
+      if (last >= nproc && tile * kCarryTile < nproc && cout && !prod.drop_top())
+        atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
     }
   }
   __syncthreads();
@@ -448,6 +543,29 @@ cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int
   ChunkProducer prod{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks};
   carry_kernel<ChunkProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
                                                                                      0, 0, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
+                             uint64_t *out, long long *top, int64_t *result, const ScanState &ss, cudaStream_t st) {
+  const uint64_t n = na > nb ? na : nb;
+  const bool sub = sa != sb;
+  const uint64_t nproc = sub ? n : n + 1;
+  const uint64_t tiles = carry_tiles(nproc);
+  if (tiles == 0 || tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  SumProducer prod{a, b, na, nb, n, sub ? top : nullptr};
+  if (sub) {
+    cudaError_t e = cudaMemsetAsync(top, 0xff, sizeof(long long), st);
+    if (e != cudaSuccess) return e;
+    const uint64_t blocks = (n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8;
+    top_diff_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(a, na, b, nb, n, top);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  carry_kernel<SumProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                   0, 0, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_finish_kernel<<<1, 256, 0, st>>>(out, nproc, prod, sa, sb, result);
   return cudaGetLastError();
 }
 

@@ -52,6 +52,13 @@ uint64_t product_workspace_bytes(uint64_t nx, uint64_t ny, bool square);
 // so that none needs more than ws_cap_bytes of workspace.
 int plan_batch(const ProductDesc *items, size_t n, uint64_t ws_cap_bytes, BatchPlan &bp);
 
+// sa |a| + sb |b| into out[0, nout) over the whole GPU (nout >= max(na,
+// nb) + 1; limbs past the sum are zeroed); (sign, size) into result[0, 2)
+// on the device.  Uses the library's carry-scan state, ordered like the
+// products' workspace.
+int large_sum_device(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
+                     uint64_t *out, uint64_t nout, int64_t *result, cudaStream_t st);
+
 // Enqueue a planned batch on st: clear its scan state, zero the empty
 // products, run every group.  Takes no lock and allocates nothing.
 int enqueue_batch(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st);

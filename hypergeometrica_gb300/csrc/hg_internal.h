@@ -132,6 +132,11 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
 cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int logN, uint64_t chunk,
                                     uint64_t nchunks, const CrtConst &cc, uint64_t *out, uint64_t nproc,
                                     const ScanState &ss, cudaStream_t st, uint64_t *tiles_used);
+// sa |a| + sb |b| into out[0, n + 1) (n = max(na, nb); out[0, n) when the
+// signs differ) over the whole GPU, with the carry scan of the products;
+// result = (sign, size).  top is one device word of scratch.
+cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
+                             uint64_t *out, long long *top, int64_t *result, const ScanState &ss, cudaStream_t st);
 // Zero out[N, nout) of every product (out[0, nout) when N == 0).
 cudaError_t launch_zero_tails(const ProductDesc *batch, uint64_t nprod, uint64_t N, cudaStream_t st);
 cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out,

@@ -32,11 +32,27 @@ struct SumDesc {
   uint64_t *out;
   uint64_t nout;
   int64_t sa, sb;
+  int64_t *res;  // (sign, size)
 };
+
+// Sums of at least this many limbs run over the whole GPU (large_sum_device)
+// instead of in one CTA.
+constexpr uint64_t kLargeSum = uint64_t(1) << 15;
 
 struct VecDesc {
   const uint64_t *p;
   uint64_t n;
+};
+
+// Descriptors of a launch: a device array, or up to kInline of them carried
+// in the kernel's parameters (no allocation or copy for small batches, whose
+// cost is then one launch).
+constexpr int kInline = 32;
+template <class Desc>
+struct Descs {
+  const Desc *p;  // device array, or null: use inl
+  Desc inl[kInline];
+  __device__ __forceinline__ Desc operator[](uint64_t i) const { return p ? p[i] : inl[i]; }
 };
 
 // Highest index < n whose limb is nonzero (or differs between a and b when
@@ -53,7 +69,11 @@ __device__ long long top_index(const uint64_t *a, uint64_t na, const uint64_t *b
       if (x != y) atomicMax(&s_top, static_cast<long long>(i));
     }
     __syncthreads();
-    if (s_top >= 0) break;
+    // Every thread reads the flag before any thread can move on and update
+    // it for the next chunk: the CTA leaves the loop together.
+    const bool found = s_top >= 0;
+    __syncthreads();
+    if (found) break;
     hi = lo;
   }
   const long long t = s_top;
@@ -61,7 +81,7 @@ __device__ long long top_index(const uint64_t *a, uint64_t na, const uint64_t *b
   return t;
 }
 
-__global__ void __launch_bounds__(kSumThreads) sum_kernel(const SumDesc *descs, int64_t *result) {
+__global__ void __launch_bounds__(kSumThreads) sum_kernel(const Descs<SumDesc> descs) {
   const SumDesc d = descs[blockIdx.x];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const uint64_t n = d.na > d.nb ? d.na : d.nb;
@@ -74,8 +94,8 @@ __global__ void __launch_bounds__(kSumThreads) sum_kernel(const SumDesc *descs, 
     if (t < 0) {  // equal magnitudes: zero
       for (uint64_t i = tid; i < d.nout; i += kSumThreads) d.out[i] = 0;
       if (tid == 0) {
-        result[2 * blockIdx.x] = 1;
-        result[2 * blockIdx.x + 1] = 0;
+        d.res[0] = 1;
+        d.res[1] = 0;
       }
       return;
     }
@@ -158,12 +178,12 @@ __global__ void __launch_bounds__(kSumThreads) sum_kernel(const SumDesc *descs, 
   }
   if (tid == 0) {
     const int64_t size = s_top + 1;
-    result[2 * blockIdx.x] = size ? sign : 1;
-    result[2 * blockIdx.x + 1] = size;
+    d.res[0] = size ? sign : 1;
+    d.res[1] = size;
   }
 }
 
-__global__ void __launch_bounds__(kSumThreads) trim_kernel(const VecDesc *descs, uint64_t *sizes) {
+__global__ void __launch_bounds__(kSumThreads) trim_kernel(const Descs<VecDesc> descs, uint64_t *sizes) {
   const VecDesc d = descs[blockIdx.x];
   const long long t = top_index(d.p, d.n, nullptr, 0, d.n);
   if (threadIdx.x == 0) sizes[blockIdx.x] = static_cast<uint64_t>(t + 1);
@@ -173,7 +193,7 @@ __global__ void __launch_bounds__(kSumThreads) trim_kernel(const VecDesc *descs,
 // products, one thread each: column k of the product is the 192-bit sum of
 // x_i y_(k-i) plus the carry from column k - 1 (< 2^71 for <= 64-limb
 // operands).
-__global__ void small_mul_kernel(const ProductDesc *descs, uint64_t n) {
+__global__ void small_mul_kernel(const Descs<ProductDesc> descs, uint64_t n) {
   const uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (k >= n) return;
   const ProductDesc d = descs[k];
@@ -217,12 +237,21 @@ template <class Desc, class Launch>
 int run_batch(const Desc *host, size_t n, cudaStream_t st, const char *what, Launch launch) {
   if (n == 0) return HG_OK;
   if (n > 0x7fffffffull) return lib_fail(HG_ERR_ARG, "%s: %zu integers exceed one launch", what, n);
+  if (n <= static_cast<size_t>(kInline)) {
+    Descs<Desc> d{};
+    for (size_t k = 0; k < n; ++k) d.inl[k] = host[k];
+    launch(d, static_cast<unsigned>(n));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? HG_OK : lib_cuda_fail(e, what);
+  }
   Desc *dev = nullptr;
   cudaError_t e = cudaMallocAsync(&dev, n * sizeof(Desc), st);
   if (e != cudaSuccess) return lib_cuda_fail(e, what);
   e = cudaMemcpyAsync(dev, host, n * sizeof(Desc), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
-    launch(dev, static_cast<unsigned>(n));
+    Descs<Desc> d{};
+    d.p = dev;
+    launch(d, static_cast<unsigned>(n));
     e = cudaGetLastError();
   }
   const cudaError_t f = cudaFreeAsync(dev, st);
@@ -241,7 +270,8 @@ extern "C" {
 int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *stream) {
   if (n && (!sums || !result)) return lib_fail(HG_ERR_ARG, "null pointer");
   if (!lib_ready()) return lib_fail(HG_ERR_NOT_INIT, "hg_add_batch_device: call hg_init first");
-  std::vector<SumDesc> d(n);
+  std::vector<SumDesc> d;
+  d.reserve(n);
   for (size_t k = 0; k < n; ++k) {
     const hg_sum &s = sums[k];
     if ((s.na && !s.a) || (s.nb && !s.b) || (s.nout && !s.out)) return lib_fail(HG_ERR_ARG, "sum %zu: null pointer", k);
@@ -249,11 +279,19 @@ int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *str
       return lib_fail(HG_ERR_ARG, "sum %zu: signs must be +1 or -1", k);
     const size_t need = (s.na > s.nb ? s.na : s.nb) + 1;
     if (s.nout < need) return lib_fail(HG_ERR_ARG, "sum %zu: nout = %zu cannot hold %zu limbs", k, s.nout, need);
-    d[k] = SumDesc{s.a, s.na, s.b, s.nb, s.out, s.nout, s.sa, s.sb};
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return run_batch(d.data(), n, st, "signed sums", [&](const SumDesc *dev, unsigned grid) {
-    sum_kernel<<<grid, kSumThreads, 0, st>>>(dev, result);
+  for (size_t k = 0; k < n; ++k) {
+    const hg_sum &s = sums[k];
+    if ((s.na > s.nb ? s.na : s.nb) >= kLargeSum) {
+      const int rc = large_sum_device(s.a, s.na, s.sa, s.b, s.nb, s.sb, s.out, s.nout, result + 2 * k, st);
+      if (rc) return rc;
+    } else {
+      d.push_back(SumDesc{s.a, s.na, s.b, s.nb, s.out, s.nout, s.sa, s.sb, result + 2 * k});
+    }
+  }
+  return run_batch(d.data(), d.size(), st, "signed sums", [&](const Descs<SumDesc> &dev, unsigned grid) {
+    sum_kernel<<<grid, kSumThreads, 0, st>>>(dev);
   });
 }
 
@@ -274,7 +312,7 @@ int hg_mul_small_batch_device(const hg_product *prods, size_t n, void *stream) {
     d[k] = ProductDesc{p.x, p.y, p.nx, ny, p.out, p.nout};
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return run_batch(d.data(), n, st, "small products", [&](const ProductDesc *dev, unsigned count) {
+  return run_batch(d.data(), n, st, "small products", [&](const Descs<ProductDesc> &dev, unsigned count) {
     small_mul_kernel<<<(count + 127) / 128, 128, 0, st>>>(dev, count);
   });
 }
@@ -288,7 +326,7 @@ int hg_trim_batch_device(const hg_vec *vecs, size_t n, uint64_t *sizes, void *st
     d[k] = VecDesc{vecs[k].p, vecs[k].n};
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return run_batch(d.data(), n, st, "trimmed sizes", [&](const VecDesc *dev, unsigned grid) {
+  return run_batch(d.data(), n, st, "trimmed sizes", [&](const Descs<VecDesc> &dev, unsigned grid) {
     trim_kernel<<<grid, kSumThreads, 0, st>>>(dev, sizes);
   });
 }

@@ -32,11 +32,10 @@ def _dev(a):
     return torch.from_numpy(a.view(np.int64).copy()).cuda(), a.size
 
 
-def _cases():
-    rng = np.random.default_rng(5)
+def _cases(sizes=(0, 1, 2, 7, 2047, 2048, 2049, 5000, 20000), count=60, seed=5):
+    rng = np.random.default_rng(seed)
     out = []
-    sizes = [0, 1, 2, 7, 2047, 2048, 2049, 5000, 20000]
-    for k in range(60):
+    for k in range(count):
         na = int(rng.choice(sizes))
         nb = int(rng.choice(sizes))
         a = W.limbs(10 * k + 1, na)
@@ -61,12 +60,20 @@ def _cases():
     return out
 
 
-def test_signed_sums_and_trims(hg):
+LARGE_SUM_SIZES = (0, 1, 3, 32767, 32768, 40000, 1 << 17, (1 << 20) + 3)
+
+
+@pytest.mark.parametrize("cases_args", [
+    {},                                                    # 60 sums: descriptors in device memory
+    {"count": 20},                                         # 20 sums: descriptors in the launch parameters
+    {"sizes": LARGE_SUM_SIZES, "count": 30, "seed": 9},    # large ones over the whole GPU, mixed with small
+], ids=["batch", "inline", "large"])
+def test_signed_sums_and_trims(hg, cases_args):
     import torch
 
     from hypergeometrica_gb300 import series as S
 
-    cases = _cases()
+    cases = _cases(**cases_args)
     keep, rec, want = [], [], []
     for a, b, sa, sb in cases:
         ta, na = _dev(a)
