@@ -217,7 +217,9 @@ typedef struct hg_sum {
 
 /* mpz-+ (src/mpz-ram.lisp:292-306) on n pairs at once: result[2k] receives
  * the sign of sum k (+1 for zero) and result[2k + 1] its length without high
- * zero limbs (device int64 array of 2n entries). */
+ * zero limbs (device int64 array of 2n entries).  Sums shorter than 2^15
+ * limbs run one CTA each; longer ones run one at a time over the whole GPU
+ * (a carry-lookahead scan ordered with the library's products). */
 int hg_add_batch_device(const hg_sum *sums, size_t n, int64_t *result, void *stream);
 
 /* Largest operand of hg_mul_small_batch_device. */
