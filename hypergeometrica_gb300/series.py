@@ -19,8 +19,11 @@ its two dependent ones (B_r (Q_r R_l), B_l (P_l R_r)) go to the
 device-resident multiply service; R is one batched signed sum
 (hg_add_batch_device) and P, Q, B get their sizes from one batched trim.
 P, Q, B and R of every node stay in device memory, one arena per height,
-until the parent has combined them.  Because the tree is the reference's,
-every partial, not just the root, equals the reference's.
+until the parent has combined them.  For a series given by polynomials the
+tree stops at nodes of at most 2^NODE_HEIGHT terms, each computed whole by
+one device thread (hg_series_nodes_device); a range's partial is the same
+integers however the range is split.  Because the tree is the reference's,
+every partial it holds, not just the root, equals the reference's.
 """
 
 from __future__ import annotations
@@ -33,7 +36,7 @@ from typing import Callable
 
 import numpy as np
 
-from ._lib import HGError, check, load
+from ._lib import HG_ERR_INCONSISTENT, HGError, check, load
 from .mpz import NTT_MULTIPLY_THRESHOLD, digits_from_int, int_from_digits
 
 
@@ -307,7 +310,9 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
     """binary-split (src/binary-splitting.lisp:123-133) on the GPU.  When
     `timings` is a list, one (height, nodes, seconds of products, seconds of
     sums and trims) record per height is appended to it, after a
-    ("tree", nodes, seconds) and a ("leaves", count, seconds) record."""
+    ("tree", nodes, seconds) and a ("leaves", count, seconds) record for the
+    tree's base nodes (whole nodes of up to 2^NODE_HEIGHT terms, or single
+    terms for a series without polynomials)."""
     import time
 
     import torch
@@ -347,7 +352,7 @@ def binary_split(series: Series, lower: int, upper: int, service=None, timings: 
             sign[j, cut] = ss[j, :, 0]
             size[j, cut] = ss[j, :, 1]
         if (size[:, cut] < 0).any():
-            raise HGError(-1, "series node partial exceeded its width bound")
+            raise HGError(HG_ERR_INCONSISTENT, "series node partial exceeded its width bound")
         leaf_limbs = int(size[:, cut].sum())
         h_first, arena_key = h0 + 1, h0
         if cut[0] == 0:  # the root itself
