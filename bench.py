@@ -185,6 +185,22 @@ def cpu_product_rate(log_size: int, threads: int) -> tuple[float, float]:
     return 2 * n / dt, dt
 
 
+def gmp_baseline(x, y, gpu_out) -> dict:
+    """GMP's mpz_mul on the same operands (one thread): its rate, and whether
+    its product equals the GPU's limb for limb."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gmp
+
+    if not gmp.available():
+        return {"unavailable": "libgmp not found on this host"}
+    timer = []
+    ref = gmp.mul(x, y, timer)
+    return {"value": len(ref) / timer[0], "unit": UNIT, "cores": 1, "seconds": timer[0],
+            "matches_gpu": bool(np.array_equal(ref, gpu_out))}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
@@ -690,7 +706,9 @@ def run_ours(args) -> None:
         rate, dt = cpu_product_rate(args.log_size, threads)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"one {na}x{nb}-limb product ({dt:.1f} s)", "cpu": model,
-                                "host_cores": cores}
+                                "host_cores": cores,
+                                "gmp": gmp_baseline(x, y, hout.numpy().view(np.uint64))}
+        line["correct"] = line["correct"] and line["cpu_baseline"]["gmp"].get("matches_gpu", True)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

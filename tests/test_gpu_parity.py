@@ -156,6 +156,20 @@ def test_large_products_residue_checks(hg, nx, ny, dist):
         assert _residue(got, q) == _residue(x, q) * _residue(y, q) % q, q
 
 
+def test_full_size_product_equals_gmp(hg):
+    """A 2^22 x 2^22-limb product equals GMP's mpz_mul limb for limb (a
+    third-party exact product; skipped where libgmp is missing)."""
+    import gmp
+
+    if not gmp.available():
+        pytest.skip("libgmp not installed")
+    n = 1 << 22
+    x = W.limbs(61, n, "uniform")
+    y = W.limbs(62, n, "uniform")
+    got = hg.mpz_mul_ntt(hg.MPZ(1, x), hg.MPZ(1, y)).storage
+    assert np.array_equal(got[: 2 * n], gmp.mul(x, y))
+
+
 def test_large_ones_product_exact(hg):
     """(2^(64n) - 1)^2 = 2^(128n) - 2^(64n+1) + 1: known limbs, longest carries."""
     n = 1 << 23

@@ -113,41 +113,13 @@ def test_parallel_tasks_same_result(oracle):
 
 def test_oracle_against_gmp(oracle):
     """Cross-check with GMP's mpz_mul (a third-party exact product), when the
-    GMP runtime is installed.  Prototypes follow the public GMP manual."""
-    name = ctypes.util.find_library("gmp")
-    if not name:
+    GMP runtime is installed (oracle/gmp.py)."""
+    import gmp
+
+    if not gmp.available():
         pytest.skip("libgmp not installed")
-    gmp = ctypes.CDLL(name)
-
-    class MPZ_T(ctypes.Structure):
-        _fields_ = [("alloc", ctypes.c_int), ("size", ctypes.c_int), ("d", ctypes.c_void_p)]
-
-    P = ctypes.POINTER(MPZ_T)
-    for f in ("__gmpz_init", "__gmpz_clear"):
-        getattr(gmp, f).argtypes = [P]
-    gmp.__gmpz_import.argtypes = [P, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
-                                  ctypes.c_void_p]
-    gmp.__gmpz_export.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.c_int, ctypes.c_size_t,
-                                  ctypes.c_int, ctypes.c_size_t, P]
-    gmp.__gmpz_export.restype = ctypes.c_void_p
-    gmp.__gmpz_mul.argtypes = [P, P, P]
-
-    def to_gmp(a):
-        z = MPZ_T()
-        gmp.__gmpz_init(ctypes.byref(z))
-        gmp.__gmpz_import(ctypes.byref(z), len(a), -1, 8, 0, 0, a.ctypes.data)
-        return z
-
     nx = ny = 1 << 15
     x = W.limbs(100, nx, "uniform")
     y = W.limbs(101, ny, "uniform")
-    zx, zy, zr = to_gmp(x), to_gmp(y), MPZ_T()
-    gmp.__gmpz_init(ctypes.byref(zr))
-    gmp.__gmpz_mul(ctypes.byref(zr), ctypes.byref(zx), ctypes.byref(zy))
-    out = np.zeros(nx + ny, dtype=np.uint64)
-    cnt = ctypes.c_size_t(0)
-    gmp.__gmpz_export(out.ctypes.data, ctypes.byref(cnt), -1, 8, 0, 0, ctypes.byref(zr))
-    for z in (zx, zy, zr):
-        gmp.__gmpz_clear(ctypes.byref(z))
     got = oracle.mpz_mul_ntt(x, y)
-    assert np.array_equal(got[: nx + ny], out)
+    assert np.array_equal(got[: nx + ny], gmp.mul(x, y))
