@@ -2,8 +2,6 @@
 modelled on the reference's suite (tests/mpz.lisp, tests/ntt.lisp,
 tests/arithmetic.lisp, tests/multiplication.lisp)."""
 
-import ctypes
-import ctypes.util
 
 import numpy as np
 import pytest
