@@ -119,6 +119,9 @@ struct DevBuf {
   uint64_t *u64() const { return static_cast<uint64_t *>(p); }
 };
 
+// Column slices of an operand upload from host memory (ntt_product_device).
+constexpr int kUploadSlices = 4;
+
 struct Context {
   bool ready = false;
   int device = 0;
@@ -133,8 +136,9 @@ struct Context {
   unsigned long long ticket_count = 0;
   uint32_t epoch = 0;
   cudaEvent_t ws_done = nullptr;
-  cudaStream_t copy_stream = nullptr;  // host entry points: upload of the second operand
+  cudaStream_t copy_stream = nullptr;  // host entry points: operand uploads
   cudaEvent_t copy_done = nullptr;
+  cudaEvent_t slice_done[2][kUploadSlices] = {};  // per operand, per column slice of the upload
   bool ws_pending = false;
   std::recursive_mutex mu;
 };
@@ -304,6 +308,8 @@ int init_locked(const uint64_t *moduli, int k, int device) {
   HG_CUDA(cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming), "event creation");
   HG_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking), "stream creation");
   HG_CUDA(cudaEventCreateWithFlags(&c.copy_done, cudaEventDisableTiming), "event creation");
+  for (auto &op : c.slice_done)
+    for (cudaEvent_t &e : op) HG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event creation");
   HG_CUDA(c.misc.ensure(64), "scan state allocation");
   HG_CUDA(cudaMemset(c.misc.p, 0, 64), "scan state init");
   c.ready = true;
@@ -654,13 +660,42 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   return HG_OK;
 }
 
+// Operands the host entry points still hold in host memory.  Given these,
+// ntt_product_device copies them into its device operands x, y itself, so
+// that the copies overlap the first forward pass.
+struct HostOperands {
+  const uint64_t *hx, *hy;  // hy null for a square
+};
+
+
+// Copy columns [c0, c1) of every row of the first strided pass (row r holds
+// limbs [r S, (r + 1) S)) of n host limbs into dst: one 2-D copy for the
+// full rows, one copy for the part of the last row below n.
+cudaError_t copy_columns(uint64_t *dst, const uint64_t *src, uint64_t n, uint64_t S, uint64_t c0, uint64_t c1,
+                         cudaStream_t st) {
+  const uint64_t full = n / S;
+  cudaError_t e = cudaSuccess;
+  if (full && c1 > c0)
+    e = cudaMemcpy2DAsync(dst + c0, S * sizeof(uint64_t), src + c0, S * sizeof(uint64_t), (c1 - c0) * sizeof(uint64_t),
+                          full, cudaMemcpyHostToDevice, st);
+  const uint64_t base = full * S;
+  if (e == cudaSuccess && base + c0 < n) {
+    const uint64_t end = std::min(base + c1, n);
+    e = cudaMemcpyAsync(dst + base + c0, src + base + c0, (end - base - c0) * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                        st);
+  }
+  return e;
+}
+
 // |x| * |y| (or |x|^2 when y == nullptr) into out[0, nout) on device memory.
 // An unbalanced pair runs in chunks (chunk_product_device).
-// When y_ready is given (two operands), operand 1's limbs may still be in
-// flight: the first strided pass runs for operand 0 alone, then waits for the
-// event and runs for operand 1, so that an upload of y overlaps it.
+// With host operands (x, y are then the device buffers to fill), each
+// operand is copied on the copy stream in column slices of the first strided
+// pass, and that pass runs slice by slice as the copies land: only one slice
+// of the upload is left exposed.  A chunked product copies x ahead of its
+// work and y on the copy stream (chunk_product_device waits for y).
 int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64_t ny, uint64_t *out, uint64_t nout,
-                       cudaStream_t st, cudaEvent_t y_ready = nullptr) {
+                       cudaStream_t st, const HostOperands *host = nullptr) {
   Context &c = g_ctx;
   const bool square = (y == nullptr);
   if (square) ny = nx;
@@ -673,8 +708,18 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     return HG_OK;
   }
   ChunkPlan cp;
-  if (!square && plan_chunks(std::max(nx, ny), std::min(nx, ny), cp))
+  if (!square && plan_chunks(std::max(nx, ny), std::min(nx, ny), cp)) {
+    cudaEvent_t y_ready = nullptr;
+    if (host) {
+      HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(x), host->hx, nx * 8, cudaMemcpyHostToDevice, st),
+              "operand upload");
+      HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(y), host->hy, ny * 8, cudaMemcpyHostToDevice, c.copy_stream),
+              "operand upload");
+      HG_CUDA(cudaEventRecord(c.copy_done, c.copy_stream), "operand upload");
+      y_ready = c.copy_done;
+    }
     return chunk_product_device(x, nx, y, ny, out, nout, cp, st, y_ready);
+  }
   const int L = ilog2_ceil(size);
   int rc = check_len(L);
   if (rc) return rc;
@@ -696,19 +741,53 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   a.limbs[1] = square ? nullptr : y;
   a.nlimbs[0] = nx;
   a.nlimbs[1] = square ? 0 : ny;
-  if (y_ready && !square && plan.size() > 1) {
-    PassArgs a0 = a, a1 = a, rest = a;
-    a0.nops = a1.nops = 1;
-    a1.data[0] = c.B.u64();
-    a1.limbs[0] = y;
-    a1.nlimbs[0] = ny;
-    HG_CUDA(run_strided_range(a0, plan, false, 0, 1, st), "forward transform");
-    HG_CUDA(cudaStreamWaitEvent(st, y_ready, 0), "operand upload ordering");
-    HG_CUDA(run_strided_range(a1, plan, false, 0, 1, st), "forward transform");
+  if (host && plan.size() == 1) {  // one contiguous pass reads the limbs: copy them first
+    HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(x), host->hx, nx * 8, cudaMemcpyHostToDevice, st),
+            "operand upload");
+    if (!square)
+      HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(y), host->hy, ny * 8, cudaMemcpyHostToDevice, st),
+              "operand upload");
+  }
+  if (host && plan.size() > 1) {
+    // The first strided pass covers one block of N = R S residues; its tile t
+    // reads columns [t C, (t + 1) C) (C = 4096 / R) of every row.
+    const PassPlan &p0 = plan[0];
+    const uint64_t S = uint64_t(1) << p0.logS;
+    const uint64_t C = uint64_t(1) << (kTileBits - p0.logR);
+    const uint64_t ntiles = N >> kTileBits;
+    const int K = static_cast<int>(std::min<uint64_t>(kUploadSlices, ntiles));
+    const int nops = square ? 1 : 2;
+    for (int op = 0; op < nops; ++op)
+      for (int k = 0; k < K; ++k) {
+        const uint64_t t0 = ntiles * k / K, t1 = ntiles * (k + 1) / K;
+        HG_CUDA(copy_columns(const_cast<uint64_t *>(op ? y : x), op ? host->hy : host->hx, op ? ny : nx, S, t0 * C,
+                             t1 * C, c.copy_stream),
+                "operand upload");
+        HG_CUDA(cudaEventRecord(c.slice_done[op][k], c.copy_stream), "operand upload");
+      }
+    const uint64_t *ptw = pass_twiddles(p0.logR + p0.logS, p0.logR, false, st);
+    for (int op = 0; op < nops; ++op)
+      for (int k = 0; k < K; ++k) {
+        const uint64_t t0 = ntiles * k / K, t1 = ntiles * (k + 1) / K;
+        HG_CUDA(cudaStreamWaitEvent(st, c.slice_done[op][k], 0), "operand upload ordering");
+        PassArgs f = a;
+        f.nops = 1;
+        f.data[0] = op ? c.B.u64() : c.A.u64();
+        f.limbs[0] = op ? y : x;
+        f.nlimbs[0] = op ? ny : nx;
+        f.logR = p0.logR;
+        f.logS = p0.logS;
+        f.logT = p0.logT;
+        f.tile_lo = t0;
+        f.tiles = t1 - t0;
+        f.ptw = ptw;
+        ProfScope ps(HG_KC_NTT_FORWARD, st, pass_bytes(f, 1, 1) * static_cast<double>(t1 - t0) / ntiles);
+        HG_CUDA(launch_ntt_strided(f, false, st), "forward transform");
+      }
+    PassArgs rest = a;
     rest.limbs[0] = rest.limbs[1] = nullptr;
     HG_CUDA(run_strided_range(rest, plan, false, 1, static_cast<int>(plan.size()) - 1, st), "forward transform");
   } else {
-    if (y_ready) HG_CUDA(cudaStreamWaitEvent(st, y_ready, 0), "operand upload ordering");
     HG_CUDA(run_strided(a, plan, false, st), "forward transform");
   }
   {
@@ -924,19 +1003,18 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
   const uint64_t *dx = static_cast<const uint64_t *>(pinned_view(x));
   const uint64_t *dy = two ? static_cast<const uint64_t *>(pinned_view(y)) : nullptr;
   uint64_t *dout = static_cast<uint64_t *>(const_cast<void *>(pinned_view(out)));
-  // A two-operand NTT product with strided passes copies its operands over
-  // the host link instead of reading them in place: x first, then y on the
-  // copy stream while the first pass transforms x.
-  cudaEvent_t y_ready = nullptr;
-  if (kind == Kind::Ntt && ilog2_ceil(size) > kTileBits) {
+  // An NTT product or square with strided passes copies its operands over
+  // the host link instead of reading them in place; ntt_product_device
+  // overlaps the copies with the first forward pass.
+  const bool host_ops = (kind == Kind::Ntt || kind == Kind::Square) && ilog2_ceil(size) > kTileBits;
+  const HostOperands ho{x, kind == Kind::Ntt ? y : nullptr};
+  if (host_ops) {
     HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
-    HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
-    HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
-    HG_CUDA(cudaMemcpyAsync(c.Y.p, y, ny * 8, cudaMemcpyHostToDevice, c.copy_stream), "operand upload");
-    HG_CUDA(cudaEventRecord(c.copy_done, c.copy_stream), "operand upload");
     dx = c.X.u64();
-    dy = c.Y.u64();
-    y_ready = c.copy_done;
+    if (kind == Kind::Ntt) {
+      HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
+      dy = c.Y.u64();
+    }
   }
   if (!dx) {
     HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
@@ -954,8 +1032,8 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
     dout = c.OUT.u64();
   }
   switch (kind) {
-    case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st, y_ready); break;
-    case Kind::Square: rc = ntt_product_device(dx, nx, nullptr, 0, dout, nd, st); break;
+    case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st, host_ops ? &ho : nullptr); break;
+    case Kind::Square: rc = ntt_product_device(dx, nx, nullptr, 0, dout, nd, st, host_ops ? &ho : nullptr); break;
     case Kind::Schoolboy: rc = small_product_device(dx, nx, dy, ny, 0, dout, nd, st); break;
     case Kind::Digit: rc = small_product_device(dx, nx, nullptr, 0, d, dout, nd, st); break;
   }
@@ -1392,6 +1470,11 @@ int hg_shutdown(void) {
   if (c.ws_done) cudaEventDestroy(c.ws_done);
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   if (c.copy_done) cudaEventDestroy(c.copy_done);
+  for (auto &op : c.slice_done)
+    for (cudaEvent_t &e : op) {
+      if (e) cudaEventDestroy(e);
+      e = nullptr;
+    }
   c.stream = nullptr;
   c.ws_done = nullptr;
   c.copy_stream = nullptr;

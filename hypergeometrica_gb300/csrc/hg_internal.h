@@ -62,7 +62,8 @@ struct PassArgs {
   uint64_t prime_stride;       // words between the arrays of consecutive primes
   uint64_t nprod;              // products in the launch
   uint64_t ws_stride;          // words between consecutive products' arrays
-  uint64_t tiles;              // tiles per (product, operand, prime)
+  uint64_t tiles;              // tiles per (product, operand, prime) in this launch
+  uint64_t tile_lo;            // strided passes: the launch covers tiles [tile_lo, tile_lo + tiles)
   PrimeConst pc[kPrimes];
   NttTables tb[kPrimes];
   // Strided passes: the inter-pass twiddles w_M^(+-s * bitrev r) of this

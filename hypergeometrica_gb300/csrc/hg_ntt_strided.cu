@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const Pass
   const int op = static_cast<int>(bid % P.nops);
   bid /= P.nops;
   const uint64_t prod = bid / P.tiles;
-  const uint64_t tile = bid % P.tiles;
+  const uint64_t tile = P.tile_lo + bid % P.tiles;
 
   const uint64_t p = P.pc[prime].p;
   const uint32_t c = P.pc[prime].c;
