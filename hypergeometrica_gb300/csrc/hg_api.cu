@@ -160,13 +160,13 @@ struct Profile {
 };
 Profile g_prof;
 
-// Counts one kernel launch of class `cls` moving `bytes` algorithmic bytes,
-// bracketed by a CUDA event pair on `st` while recording is on.
+// Counts `launches` kernel launches of class `cls` moving `bytes` algorithmic
+// bytes, bracketed by a CUDA event pair on `st` while recording is on.
 class ProfScope {
  public:
-  ProfScope(int cls, cudaStream_t st, double bytes) : cls_(cls), st_(st) {
+  ProfScope(int cls, cudaStream_t st, double bytes, int launches = 1) : cls_(cls), st_(st) {
     std::lock_guard<std::mutex> lk(g_prof.mu);
-    g_prof.launches[cls]++;
+    g_prof.launches[cls] += launches;
     g_prof.bytes[cls] += bytes;
     if (g_prof.on && cudaEventCreate(&b_) == cudaSuccess) cudaEventRecord(b_, st_);
   }
@@ -651,7 +651,7 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   if (rc) return rc;
   uint64_t tiles = 0;
   {
-    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(size));
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(size), 2);  // local scan + fix
     HG_CUDA(launch_crt_carry_chunks(c.A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L), out, size, ss, st,
                                     &tiles),
             "reconstruction");
@@ -805,7 +805,7 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   if (rc) return rc;
   uint64_t tiles = 0;
   {
-    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(nproc));
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(nproc), 2);  // local scan + fix
     HG_CUDA(launch_crt_carry(c.A.u64(), L, crt_const(L), out, nout, ss, st, &tiles), "reconstruction");
   }
   HG_CUDA(ws_release(st), "workspace ordering");
@@ -932,7 +932,7 @@ int small_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   if (rc) return rc;
   uint64_t tiles = 0;
   {
-    ProfScope ps(HG_KC_SMALL, st, 8.0 * static_cast<double>(nx + (y ? ny : 0) + size));
+    ProfScope ps(HG_KC_SMALL, st, 8.0 * static_cast<double>(nx + (y ? ny : 0) + size), 2);
     if (y)
       HG_CUDA(launch_schoolboy_carry(x, nx, y, ny, out, size, ss, st, &tiles), "schoolboy product");
     else
@@ -1375,7 +1375,8 @@ int large_sum_device(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t 
   if (rc) return rc;
   long long *top = reinterpret_cast<long long *>(static_cast<char *>(g_ctx.misc.p) + 16);
   {
-    ProfScope ps(HG_KC_OTHER, st, 24.0 * static_cast<double>(nproc));
+    // (top search,) local scan, fix, sign and size
+    ProfScope ps(HG_KC_OTHER, st, 24.0 * static_cast<double>(nproc), sa != sb ? 4 : 3);
     HG_CUDA(launch_large_sum(a, na, sa, b, nb, sb, out, top, result, ss, st), "large sum");
   }
   HG_CUDA(ws_release(st), "workspace ordering");

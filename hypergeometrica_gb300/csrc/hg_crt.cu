@@ -7,10 +7,13 @@
 // reconstruction gives the same limbs.  Here Garner's mixed radix
 // (src/modular-arithmetic.lisp:235-267) produces each coefficient as three
 // limbs V_i = y0 + p0 t1 + p0 p1 t2, the overlap-add sum_i V_i 2^(64 i) is
-// formed per position, and carries are resolved by a carry-lookahead scan:
-// within a CTA by warp shuffles, across CTAs by decoupled look-back on
-// per-tile flags.  Every wait is bounded; a wait that runs out latches
-// kDevTimeout in the device error word instead of spinning forever.
+// formed per position, and carries are resolved by a carry-lookahead scan
+// within a CTA by warp shuffles.  Across CTAs a single product's tiles are
+// written with carry-in 0 and then fixed by a second launch that composes
+// the tiles' (generate, propagate) aggregates; a batch of products resolves
+// them by decoupled look-back on per-tile flags in one launch.  Every wait
+// is bounded; a wait that runs out latches kDevTimeout in the device error
+// word instead of spinning forever.
 //
 // The same overlap-add + scan finishes the schoolboy and by-digit products
 // (src/mpz-ram.lisp:367-431), with V_i = sum_j x_(i-j) y_j.
@@ -74,7 +77,7 @@ struct CrtProducer {
     }
   }
 
-  __device__ __forceinline__ bool drop_top() const { return false; }
+  __host__ __device__ __forceinline__ bool drop_top() const { return false; }
 
   // Residues may be any 64-bit values congruent to the coefficient (the
   // inverse leaves [0, 2p)): every one enters through a Shoup product.
@@ -113,7 +116,7 @@ struct ChunkProducer {
   uint64_t stride;      // words between consecutive chunks' residues
   uint64_t chunk, nchunks;
 
-  __device__ __forceinline__ bool drop_top() const { return false; }
+  __host__ __device__ __forceinline__ bool drop_top() const { return false; }
 
   __device__ __forceinline__ static uint64_t sum2(uint64_t a, uint64_t b, uint64_t p) {
     return (a >= p ? a - p : a) + (b >= p ? b - p : b);
@@ -172,7 +175,7 @@ struct ConvProducer {
   uint64_t ny;
   uint64_t dval;
 
-  __device__ __forceinline__ bool drop_top() const { return false; }
+  __host__ __device__ __forceinline__ bool drop_top() const { return false; }
 
   __device__ __forceinline__ void eight(uint64_t, uint64_t i0, uint64_t nproc, V3 (&v)[8]) const {
 #pragma unroll
@@ -210,7 +213,7 @@ struct SumProducer {
   uint64_t na, nb, n;
   const long long *top;  // subtraction only
 
-  __device__ __forceinline__ bool drop_top() const { return top != nullptr; }
+  __host__ __device__ __forceinline__ bool drop_top() const { return top != nullptr; }
 
   __device__ __forceinline__ bool a_larger() const {
     if (!top) return true;
@@ -359,7 +362,12 @@ __device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, uint64_t 
 // Tiles of 4096 limbs, two 512-thread CTAs per SM (64 registers): 4% faster
 // than 2048-limb tiles at four CTAs per SM, with half as many tiles in
 // flight for the look-back to cross.
-template <class Producer>
+//
+// kLocal (single products only): no look-back.  Each tile is written as if
+// its carry-in were 0 and publishes its aggregate (g, p) once; carry_fix_kernel,
+// launched next on the same stream, then adds the true carry-in.  No CTA
+// waits on another, so the tiles stream at the memory and integer-pipe rate.
+template <class Producer, bool kLocal>
 __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(const Producer prod0, uint64_t *__restrict__ out,
                                                               uint64_t nproc, ScanState ss, const ProductDesc *batch,
                                                               uint64_t tpp, uint64_t ws_stride, uint64_t n) {
@@ -459,7 +467,14 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
     excl = lane == 0 ? GP{0, 1} : GP{og, op};
   }
   excl = gp_compose(wpre, excl);  // runs over positions before this thread, within the tile
-  if (wid == 0) {
+  if (kLocal) {
+    if (tid == 0) {
+      GP agg{0, 1};
+      for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
+      reinterpret_cast<volatile unsigned long long *>(ss.flags)[gt] = flag_word(ss.epoch, 1, agg.g, agg.p);
+      s_cin = 0;
+    }
+  } else if (wid == 0) {
     GP agg{0, 1};
     for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
     const uint32_t cin = look_back_warp(ss, gt, first, agg, lane);
@@ -495,6 +510,98 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
   }
 }
 
+// The second half of a kLocal carry launch, one warp per tile.  Tile t's
+// carry-in is the composition of the aggregates of tiles t - 1, t - 2, ...
+// up to the nearest one that does not propagate (p = 0), or 0 before tile 0.
+// Every flag is final here (the local launch ran to completion earlier on
+// the stream), so nothing waits; a flag of another launch is an error.
+// A warp reads 128 predecessors per round, four per lane.
+//
+// A carry-in of 1 changes only the tile's leading run of positions that
+// propagate.  p at a position means A = 2^64 - 1 with no carry out (A is
+// the position's sum before carries, and a carry out of it leaves at most 1,
+// so A = 2^64 - 1 always propagates), and the local launch wrote exactly A
+// there: the run is the tile's leading limbs equal to 2^64 - 1.  They become
+// 0 and the first limb after them gains 1; a tile that is one run becomes 0
+// and passes the carry on, as its p = 1 aggregate already says.
+constexpr int kFixWarps = 8;
+
+__global__ void __launch_bounds__(kFixWarps * 32) carry_fix_kernel(uint64_t *out, uint64_t nproc, uint64_t tiles,
+                                                                   ScanState ss, bool drop_top) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t t = static_cast<uint64_t>(blockIdx.x) * kFixWarps + (threadIdx.x >> 5);
+  if (t >= tiles) return;
+  const unsigned long long *flags = ss.flags;
+  auto gp_of = [&](unsigned long long w, bool &bad) {
+    if ((w >> 32) != ss.epoch || (w & 3u) != 1u) bad = true;
+    return GP{static_cast<uint32_t>((w >> 2) & 1u), static_cast<uint32_t>((w >> 3) & 1u)};
+  };
+  GP acc{0, 1};
+  bool bad = false;
+  for (int64_t hi = static_cast<int64_t>(t) - 1;; hi -= 128) {
+    // Lane l composes tiles hi - 4l (most significant) down to hi - 4l - 3;
+    // positions before tile 0 emit carry 0.
+    GP mine{0, 1};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t j = hi - 4 * lane - q;
+      const GP f = j >= 0 ? gp_of(flags[j], bad) : GP{0, 0};
+      mine = gp_compose(f, mine);
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+      if (lane == 0) atomicCAS(ss.err, kDevOk, kDevTicket);
+      return;
+    }
+    // Lane 0 most significant, lane 31 least.
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t og = __shfl_down_sync(0xffffffffu, mine.g, d);
+      const uint32_t op = __shfl_down_sync(0xffffffffu, mine.p, d);
+      if (lane + d < 32) mine = gp_compose(GP{og, op}, mine);
+    }
+    const GP win{__shfl_sync(0xffffffffu, mine.g, 0), __shfl_sync(0xffffffffu, mine.p, 0)};
+    acc = gp_compose(win, acc);
+    if (!acc.p) break;  // decided: a window reaching past tile 0 always ends here
+  }
+  const uint32_t cin = acc.g;
+  const uint64_t base = t * kCarryTile;
+  const uint64_t end = base + kCarryTile < nproc ? base + kCarryTile : nproc;
+  if (t == tiles - 1 && lane == 0 && !drop_top) {
+    bool b2 = false;
+    const GP own = gp_of(flags[t], b2);
+    if (own.g | (own.p & cin)) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
+  }
+  if (!cin) return;
+  for (uint64_t i = base; i < end; i += 32) {
+    const uint64_t k = i + lane;
+    const bool valid = k < end;
+    const uint64_t w = valid ? out[k] : 0;
+    const unsigned stop = __ballot_sync(0xffffffffu, valid && w != ~0ull);
+    if (!stop) {
+      if (valid) out[k] = 0;
+      continue;
+    }
+    const int f = __ffs(stop) - 1;
+    if (lane < f) out[k] = 0;
+    if (lane == f) out[k] = w + 1;
+    break;
+  }
+}
+
+template <class Producer>
+cudaError_t launch_local_carry(const Producer &prod, uint64_t *out, uint64_t nproc, uint64_t tiles, const ScanState &ss,
+                               cudaStream_t st) {
+  if (tiles == 0) return cudaSuccess;
+  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  carry_kernel<Producer, true><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
+                                                                                      0, 0, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const uint64_t blocks = (tiles + kFixWarps - 1) / kFixWarps;
+  carry_fix_kernel<<<static_cast<unsigned>(blocks), kFixWarps * 32, 0, st>>>(out, nproc, tiles, ss, prod.drop_top());
+  return cudaGetLastError();
+}
+
 // out[N, nout) = 0 for product blockIdx.x.
 __global__ void zero_tails_kernel(const ProductDesc *batch, uint64_t N) {
   const ProductDesc d = batch[blockIdx.x];
@@ -512,10 +619,7 @@ cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, 
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  CrtProducer prod{res, n, cc};
-  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                   0, 0, 0);
-  return cudaGetLastError();
+  return launch_local_carry(CrtProducer{res, n, cc}, out, nproc, tiles, ss, st);
 }
 
 cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int logN, const CrtConst &cc,
@@ -526,7 +630,7 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
   CrtProducer prod{res, n, cc};
-  carry_kernel<CrtProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, nullptr, 0, ss, batch, tpp,
+  carry_kernel<CrtProducer, false><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, nullptr, 0, ss, batch, tpp,
                                                                                    ws_stride, n);
   return cudaGetLastError();
 }
@@ -540,10 +644,8 @@ cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  ChunkProducer prod{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks};
-  carry_kernel<ChunkProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                     0, 0, 0);
-  return cudaGetLastError();
+  return launch_local_carry(ChunkProducer{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks}, out, nproc, tiles, ss,
+                            st);
 }
 
 cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
@@ -561,9 +663,7 @@ cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const u
     top_diff_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(a, na, b, nb, n, top);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  carry_kernel<SumProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                   0, 0, 0);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_local_carry(prod, out, nproc, tiles, ss, st);
   if (e != cudaSuccess) return e;
   sum_finish_kernel<<<1, 256, 0, st>>>(out, nproc, prod, sa, sb, result);
   return cudaGetLastError();
@@ -582,10 +682,7 @@ cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  ConvProducer prod{x, nx, y, ny, 0};
-  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                    0, 0, 0);
-  return cudaGetLastError();
+  return launch_local_carry(ConvProducer{x, nx, y, ny, 0}, out, nproc, tiles, ss, st);
 }
 
 cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,
@@ -594,10 +691,7 @@ cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint6
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  ConvProducer prod{x, nx, nullptr, 1, d};
-  carry_kernel<ConvProducer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                    0, 0, 0);
-  return cudaGetLastError();
+  return launch_local_carry(ConvProducer{x, nx, nullptr, 1, d}, out, nproc, tiles, ss, st);
 }
 
 }  // namespace hg
