@@ -1,13 +1,13 @@
-"""GMP's mpz_mul through ctypes: a third-party exact product, for checking and
-timing beside the oracle.  Test infrastructure, like the rest of this
+"""GMP's mpz_mul and mpz_ui_pow_ui through ctypes: third-party exact
+products and powers, for checking and timing beside the oracle.  Test infrastructure, like the rest of this
 directory: tests and bench.py's CPU-baseline leg use it to compare against
 or to time; nothing on the product path does.
 
 GMP's runtime (libgmp.so.10) ships with gcc, so it is on both the build
 machine and the GPU host; its headers are not, so the prototypes below are
 declared by hand from the public GMP manual (mpz_init, mpz_clear,
-mpz_import, mpz_export, mpz_mul; __mpz_struct is {int alloc; int size;
-limb pointer}).
+mpz_import, mpz_export, mpz_mul, mpz_ui_pow_ui; __mpz_struct is {int alloc;
+int size; limb pointer}).
 """
 
 from __future__ import annotations
@@ -41,6 +41,7 @@ def _load():
                                     ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t, P]
         g.__gmpz_export.restype = ctypes.c_void_p
         g.__gmpz_mul.argtypes = [P, P, P]
+        g.__gmpz_ui_pow_ui.argtypes = [P, ctypes.c_ulong, ctypes.c_ulong]
         _lib = g
     return _lib
 
@@ -80,3 +81,29 @@ def mul(x: np.ndarray, y: np.ndarray, timer=None) -> np.ndarray:
     for z in (zx, zy, zr):
         g.__gmpz_clear(ctypes.byref(z))
     return out[: len(x) + len(y)]
+
+
+def _export(g, z: _MPZ, nlimbs: int) -> np.ndarray:
+    out = np.zeros(nlimbs, dtype=np.uint64)
+    cnt = ctypes.c_size_t(0)
+    g.__gmpz_export(out.ctypes.data, ctypes.byref(cnt), -1, 8, 0, 0, ctypes.byref(z))
+    return out[: cnt.value]
+
+
+def ui_pow_ui(base: int, exp: int, timer=None) -> np.ndarray:
+    """base ** exp as little-endian uint64 limbs, without high zero limbs.
+    With `timer` (a list), the seconds spent in mpz_ui_pow_ui are appended."""
+    import math
+    import time
+
+    g = _load()
+    z = _MPZ()
+    g.__gmpz_init(ctypes.byref(z))
+    t = time.perf_counter()
+    g.__gmpz_ui_pow_ui(ctypes.byref(z), base, exp)
+    if timer is not None:
+        timer.append(time.perf_counter() - t)
+    bits = int(exp * math.log2(base)) + 2 if base > 1 else 1
+    out = _export(g, z, bits // 64 + 2)
+    g.__gmpz_clear(ctypes.byref(z))
+    return out

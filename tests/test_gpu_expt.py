@@ -2,8 +2,10 @@
 
 9^(9^9) has 1,228,093,895 bits (the reference's log of that run,
 logs/24apr21-999-ram.txt:224).  The device result must have exactly that
-length and the residues of pow(9, 9^9, m) for independent primes m; smaller
-powers are compared with Python's exact integers.
+length and the residues of pow(9, 9^9, m) for independent primes m, and its
+limbs must equal GMP's mpz_ui_pow_ui(9, 9^9) (a third-party exact power;
+skipped where libgmp is missing).  Smaller powers are compared with
+Python's exact integers.
 """
 
 import numpy as np
@@ -37,3 +39,16 @@ def test_nine_to_nine_to_nine(hg):
     v = int_from_digits(x.t[: x.size].cpu().numpy().view(np.uint64))
     for m in ((1 << 61) - 1, 1000000007, 2**89 - 1):
         assert v % m == pow(9, 9**9, m)
+
+
+def test_nine_to_nine_to_nine_equals_gmp(hg):
+    import gmp
+
+    from hypergeometrica_gb300 import series as S
+
+    if not gmp.available():
+        pytest.skip("libgmp not installed")
+    want = gmp.ui_pow_ui(9, 9**9)
+    x = S.mpz_expt_device(9, 9**9)
+    assert x.size == want.size
+    assert np.array_equal(x.t[: x.size].cpu().numpy().view(np.uint64), want)

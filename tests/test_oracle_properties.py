@@ -121,3 +121,16 @@ def test_oracle_against_gmp(oracle):
     y = W.limbs(101, ny, "uniform")
     got = oracle.mpz_mul_ntt(x, y)
     assert np.array_equal(got[: nx + ny], gmp.mul(x, y))
+
+
+def test_gmp_powers_against_python():
+    """The GMP power binding (oracle/gmp.py) that the 9^(9^9) GPU check
+    compares with: exact against Python's integers on small powers."""
+    import gmp
+
+    from hypergeometrica_gb300.mpz import int_from_digits
+
+    if not gmp.available():
+        pytest.skip("libgmp not installed")
+    for base, exp in ((9, 9**5), (3, 1000), (2**32 - 5, 77), (7, 1), (2, 64), (5, 0)):
+        assert int_from_digits(gmp.ui_pow_ui(base, exp)) == base**exp
