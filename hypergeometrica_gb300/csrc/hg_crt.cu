@@ -85,9 +85,11 @@ struct CrtProducer {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
     const uint64_t y0 = shoup_mul(r0, k.k0.x, k.k0.y, p0, c0);
-    const uint64_t t1 = sub_mod(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);
-    uint64_t t2 = sub_mod(shoup_mul(r2, k.k2a.x, k.k2a.y, p2, c2), shoup_mul(y0, k.k2b.x, k.k2b.y, p2, c2), p2);
-    t2 = sub_mod(t2, shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
+    const uint64_t t1 =
+        sub_mod_borrow(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);
+    uint64_t t2 =
+        sub_mod_borrow(shoup_mul(r2, k.k2a.x, k.k2a.y, p2, c2), shoup_mul(y0, k.k2b.x, k.k2b.y, p2, c2), p2);
+    t2 = sub_mod_borrow(t2, shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
     // V = y0 + p0 t1 + (p0 p1) t2 < p0 p1 p2 < 2^188
     V3 v{y0, 0, 0};
     add128_to(v, p0 * t1, __umul64hi(p0, t1));
@@ -119,7 +121,7 @@ struct ChunkProducer {
   __host__ __device__ __forceinline__ bool drop_top() const { return false; }
 
   __device__ __forceinline__ static uint64_t sum2(uint64_t a, uint64_t b, uint64_t p) {
-    return (a >= p ? a - p : a) + (b >= p ? b - p : b);
+    return fold_p(a, p) + fold_p(b, p);
   }
 
   __device__ __forceinline__ uint64_t sum_res(const uint64_t *r0, const uint64_t *r1, int j) const {

@@ -106,10 +106,10 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__re
           v[i | (1 << j)] = shoup_mul(u - w + p, t.x, t.y, p, c);  // u - w + p in (0, 2p)
         }
       } else {
-        const uint64_t uu = u >= p ? u - p : u;
+        const uint64_t uu = fold_p(u, p);
         uint64_t t;
         if (trivial) {
-          t = w >= p ? w - p : w;
+          t = fold_p(w, p);
         } else {
           const ulonglong2 tt = tw[ts ^ swz_tw(rp << sh)];
           t = shoup_mul(w, tt.x, tt.y, p, c);

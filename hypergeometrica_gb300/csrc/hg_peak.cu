@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(256) peak_kernel(uint64_t *sink, PrimeConst pc
           v[i] = add_mod(u, x, p);
           v[i | (1 << j)] = shoup_mul(u - x + p, t.x, t.y, p, c);
         } else {
-          const uint64_t uu = u >= p ? u - p : u;
+          const uint64_t uu = fold_p(u, p);
           const uint64_t y = shoup_mul(x, t.x, t.y, p, c);
           v[i] = uu + y;
           v[i | (1 << j)] = uu - y + p;
