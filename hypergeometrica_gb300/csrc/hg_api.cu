@@ -951,7 +951,6 @@ int read_device_error(cudaStream_t st) {
   if (err) {
     HG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st), "error word reset");
     HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
-    if (err == kDevTimeout) return fail(HG_ERR_TIMEOUT, "a carry look-back wait ran out; results are invalid");
     if (err == kDevCarryOverflow) return fail(HG_ERR_INCONSISTENT, "a carry left the top of the result storage");
     return fail(HG_ERR_CUDA, "device error %d", err);
   }
@@ -1160,7 +1159,7 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   ss.epoch = 1;
   ss.err = bb.err;
   {
-    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(N) * static_cast<double>(g.nprod));
+    ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(N) * static_cast<double>(g.nprod), 2);  // tiles + fix
     HG_CUDA(launch_crt_carry_batch(ws, slab, g.L, crt_const(g.L), d, g.nprod, ss, st), "reconstruction");
   }
   return HG_OK;

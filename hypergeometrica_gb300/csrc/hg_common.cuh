@@ -34,9 +34,8 @@ struct PrimeConst {
 // Device error word codes (latched with atomicCAS; first error wins).
 enum DevErr : int {
   kDevOk = 0,
-  kDevTimeout = 1,        // a look-back wait ran out of iterations
   kDevCarryOverflow = 2,  // a carry left the top of the result
-  kDevTicket = 3,         // a carry-scan tile ticket fell outside its launch
+  kDevTicket = 3,         // a carry tile ticket fell outside its launch, or a tile aggregate of another launch
 };
 
 // x - p when x >= p, else x.  The butterflies' corrections select rather

@@ -8,12 +8,10 @@
 // (src/modular-arithmetic.lisp:235-267) produces each coefficient as three
 // limbs V_i = y0 + p0 t1 + p0 p1 t2, the overlap-add sum_i V_i 2^(64 i) is
 // formed per position, and carries are resolved by a carry-lookahead scan
-// within a CTA by warp shuffles.  Across CTAs a single product's tiles are
-// written with carry-in 0 and then fixed by a second launch that composes
-// the tiles' (generate, propagate) aggregates; a batch of products resolves
-// them by decoupled look-back on per-tile flags in one launch.  Every wait
-// is bounded; a wait that runs out latches kDevTimeout in the device error
-// word instead of spinning forever.
+// within a CTA by warp shuffles.  Across CTAs each tile is written with
+// carry-in 0 and publishes its (generate, propagate) aggregate; a second
+// launch composes every tile's carry-in from the aggregates below it and
+// applies it.  No kernel here waits on another CTA.
 //
 // The same overlap-add + scan finishes the schoolboy and by-digit products
 // (src/mpz-ram.lisp:367-431), with V_i = sum_j x_(i-j) y_j.
@@ -26,7 +24,8 @@ constexpr int kCarryThreads = 512;
 constexpr int kCarryMinBlocks = 2;  // 64 registers
 constexpr int kCarryPer = 8;
 constexpr int kCarryTile = kCarryThreads * kCarryPer;
-constexpr int kSpinLimit = 1 << 22;
+
+__device__ __forceinline__ uint64_t carry_tiles_dev(uint64_t n) { return (n + kCarryTile - 1) / kCarryTile; }
 
 struct V3 {
   uint64_t w0, w1, w2;
@@ -292,91 +291,29 @@ __global__ void sum_finish_kernel(const uint64_t *out, uint64_t nproc, SumProduc
   }
 }
 
-__device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t state, uint32_t g, uint32_t p) {
-  return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | state;
+// A tile's published aggregate: the launch's epoch in the high word, then
+// p, g and the state bit 1 ("published").
+__device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t g, uint32_t p) {
+  return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | 1u;
 }
 
-// Carry into the tile from all earlier tiles, computed by one full warp.
-// Publishes this tile's aggregate first so that later tiles can proceed,
-// then reads the flags of the 32 nearest predecessors at once (lane l reads
-// tile - 1 - l), combines them with a shuffle reduction, and moves to the
-// next window of 32 until some predecessor has published its inclusive
-// carry.  Every lane's wait is bounded; a wait that runs out latches
-// kDevTimeout and the carry is taken as 0.
-__device__ uint32_t look_back_warp(const ScanState &ss, uint64_t tile, uint64_t first, GP agg, int lane) {
-  volatile unsigned long long *flags = ss.flags;
-  if (tile == first) return 0;  // the product's first tile
-  if (lane == 0) {
-    __threadfence();
-    flags[tile] = flag_word(ss.epoch, 1, agg.g, agg.p);
-  }
-  GP acc{0, 1};  // identity: carry passes through
-  int64_t hi = static_cast<int64_t>(tile) - 1;
-  const int64_t lo = static_cast<int64_t>(first);
-  for (;;) {
-    const int64_t j = hi - lane;
-    GP mine{0, 0};  // before the product's first tile: a run that emits carry 0
-    bool inclusive = true;
-    bool ok = true;
-    unsigned long long w = 0;
-    if (j >= lo) {
-      int spins = 0;
-      for (;;) {
-        w = flags[j];
-        if ((w >> 32) == ss.epoch && (w & 3u)) break;
-        if (++spins >= kSpinLimit) {
-          ok = false;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    if (__any_sync(0xffffffffu, !ok)) {
-      if (lane == 0) atomicCAS(ss.err, kDevOk, kDevTimeout);
-      return 0;
-    }
-    if (j >= lo) {
-      inclusive = (w & 3u) == 2u;
-      mine = inclusive ? GP{static_cast<uint32_t>((w >> 2) & 1u), 0u}
-                       : GP{static_cast<uint32_t>((w >> 2) & 1u), static_cast<uint32_t>((w >> 3) & 1u)};
-    }
-    const unsigned inc = __ballot_sync(0xffffffffu, inclusive);
-    const int stop = inc ? __ffs(inc) - 1 : 32;  // nearest inclusive lane
-    if (lane > stop) mine = GP{0, 1};
-    // Reduce in significance order: lane 31 least significant, lane 0 most.
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t og = __shfl_down_sync(0xffffffffu, mine.g, d);
-      const uint32_t op = __shfl_down_sync(0xffffffffu, mine.p, d);
-      if (lane + d < 32) mine = gp_compose(GP{og, op}, mine);
-    }
-    const GP win{__shfl_sync(0xffffffffu, mine.g, 0), __shfl_sync(0xffffffffu, mine.p, 0)};
-    acc = gp_compose(win, acc);
-    if (inc) return acc.g;
-    hi -= 32;
-  }
-}
-
-// One tile of 4096 output limbs per CTA.  Single product: tiles in ticket
-// order.  Batch (batch != nullptr): tickets run product-major, tpp tiles per
-// product; product k's residues are rebased by k * ws_stride, its output is
-// batch[k].out[0, min(nout, n)), and the look-back stops at its first tile.
-// Tiles of 4096 limbs, two 512-thread CTAs per SM (64 registers): 4% faster
-// than 2048-limb tiles at four CTAs per SM, with half as many tiles in
-// flight for the look-back to cross.
+// One tile of 4096 output limbs per CTA, in ticket order.  Batch (batch !=
+// nullptr): tickets run product-major, tpp tiles per product; product k's
+// residues are rebased by k * ws_stride and its output is
+// batch[k].out[0, min(nout, n)).  Tiles of 4096 limbs, two 512-thread CTAs
+// per SM (64 registers).
 //
-// kLocal (single products only): no look-back.  Each tile is written as if
-// its carry-in were 0 and publishes its aggregate (g, p) once; carry_fix_kernel,
-// launched next on the same stream, then adds the true carry-in.  No CTA
-// waits on another, so the tiles stream at the memory and integer-pipe rate.
-template <class Producer, bool kLocal>
+// Each tile is written as if its carry-in were 0 and publishes its
+// aggregate (g, p) once; carry_fix_kernel, launched next on the same
+// stream, then adds the true carry-in.  No CTA waits on another, so the
+// tiles stream at the memory and integer-pipe rate.
+template <class Producer>
 __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(const Producer prod0, uint64_t *__restrict__ out,
                                                               uint64_t nproc, ScanState ss, const ProductDesc *batch,
                                                               uint64_t tpp, uint64_t ws_stride, uint64_t n) {
   __shared__ uint64_t s_prev[kCarryThreads][9];
   __shared__ GP s_warp[kCarryThreads / 32];
   __shared__ unsigned long long s_tile;
-  __shared__ uint32_t s_cin;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
   if (tid == 0) s_tile = atomicAdd(ss.ticket, 1ull) - ss.ticket_base;
@@ -389,11 +326,10 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
   // The producer stays an unmodified kernel parameter; product k's residues
   // are addressed through an explicit word offset.
   const Producer &prod = prod0;
-  uint64_t tile = gt, first = 0, off = 0;
+  uint64_t tile = gt, off = 0;
   if (batch) {
     const uint64_t k = gt / tpp;
     tile = gt - k * tpp;
-    first = k * tpp;
     off = k * ws_stride;
     out = batch[k].out;
     nproc = batch[k].nout < n ? batch[k].nout : n;
@@ -469,29 +405,12 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
     excl = lane == 0 ? GP{0, 1} : GP{og, op};
   }
   excl = gp_compose(wpre, excl);  // runs over positions before this thread, within the tile
-  if (kLocal) {
-    if (tid == 0) {
-      GP agg{0, 1};
-      for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
-      reinterpret_cast<volatile unsigned long long *>(ss.flags)[gt] = flag_word(ss.epoch, 1, agg.g, agg.p);
-      s_cin = 0;
-    }
-  } else if (wid == 0) {
+  if (tid == 0) {
     GP agg{0, 1};
     for (int w = 0; w < kCarryThreads / 32; ++w) agg = gp_compose(agg, s_warp[w]);
-    const uint32_t cin = look_back_warp(ss, gt, first, agg, lane);
-    if (lane == 0) {
-      const uint32_t cout = agg.g | (agg.p & cin);
-      __threadfence();
-      reinterpret_cast<volatile unsigned long long *>(ss.flags)[gt] = flag_word(ss.epoch, 2, cout, 0);
-      s_cin = cin;
-      const uint64_t last = tile * kCarryTile + kCarryTile;
-      if (last >= nproc && tile * kCarryTile < nproc && cout && !prod.drop_top())
-        atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
-    }
+    ss.flags[gt] = flag_word(ss.epoch, agg.g, agg.p);
   }
-  __syncthreads();
-  uint32_t cin = excl.g | (excl.p & s_cin);
+  uint32_t cin = excl.g;  // carry-in 0 at the tile's first position
   // Stage the tile's limbs in shared memory (reusing s_prev) and store them
   // with consecutive lanes on consecutive limbs: full 256-byte segments,
   // which also suits an output that lives in host memory.
@@ -512,27 +431,39 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
   }
 }
 
-// The second half of a kLocal carry launch, one warp per tile.  Tile t's
-// carry-in is the composition of the aggregates of tiles t - 1, t - 2, ...
-// up to the nearest one that does not propagate (p = 0), or 0 before tile 0.
-// Every flag is final here (the local launch ran to completion earlier on
-// the stream), so nothing waits; a flag of another launch is an error.
-// A warp reads 128 predecessors per round, four per lane.
+// The second launch of a carry, one warp per tile.  Tile t's carry-in is
+// the composition of the aggregates of tiles t - 1, t - 2, ... up to the
+// nearest one that does not propagate (p = 0), or 0 before the product's
+// first tile.  Every flag is final here (the tile launch ran to completion
+// earlier on the stream), so nothing waits; a flag of another launch is an
+// error.  A warp reads 128 predecessors per round, four per lane.  Batches
+// (batch != nullptr) index tiles as the tile launch does.
 //
 // A carry-in of 1 changes only the tile's leading run of positions that
 // propagate.  p at a position means A = 2^64 - 1 with no carry out (A is
 // the position's sum before carries, and a carry out of it leaves at most 1,
-// so A = 2^64 - 1 always propagates), and the local launch wrote exactly A
+// so A = 2^64 - 1 always propagates), and the tile launch wrote exactly A
 // there: the run is the tile's leading limbs equal to 2^64 - 1.  They become
 // 0 and the first limb after them gains 1; a tile that is one run becomes 0
 // and passes the carry on, as its p = 1 aggregate already says.
 constexpr int kFixWarps = 8;
 
-__global__ void __launch_bounds__(kFixWarps * 32) carry_fix_kernel(uint64_t *out, uint64_t nproc, uint64_t tiles,
-                                                                   ScanState ss, bool drop_top) {
+__global__ void __launch_bounds__(kFixWarps * 32)
+    carry_fix_kernel(uint64_t *out, uint64_t nproc, uint64_t tiles, ScanState ss, bool drop_top,
+                     const ProductDesc *batch, uint64_t tpp, uint64_t n) {
   const int lane = threadIdx.x & 31;
-  const uint64_t t = static_cast<uint64_t>(blockIdx.x) * kFixWarps + (threadIdx.x >> 5);
-  if (t >= tiles) return;
+  const uint64_t gt = static_cast<uint64_t>(blockIdx.x) * kFixWarps + (threadIdx.x >> 5);
+  if (gt >= tiles) return;
+  uint64_t t = gt, first = 0;
+  if (batch) {
+    const uint64_t k = gt / tpp;
+    t = gt - k * tpp;
+    first = k * tpp;
+    out = batch[k].out;
+    nproc = batch[k].nout < n ? batch[k].nout : n;
+  }
+  const uint64_t ntiles = carry_tiles_dev(nproc);  // tiles that hold positions
+  if (t >= ntiles) return;
   const unsigned long long *flags = ss.flags;
   auto gp_of = [&](unsigned long long w, bool &bad) {
     if ((w >> 32) != ss.epoch || (w & 3u) != 1u) bad = true;
@@ -540,14 +471,14 @@ __global__ void __launch_bounds__(kFixWarps * 32) carry_fix_kernel(uint64_t *out
   };
   GP acc{0, 1};
   bool bad = false;
-  for (int64_t hi = static_cast<int64_t>(t) - 1;; hi -= 128) {
+  for (int64_t hi = static_cast<int64_t>(gt) - 1;; hi -= 128) {
     // Lane l composes tiles hi - 4l (most significant) down to hi - 4l - 3;
-    // positions before tile 0 emit carry 0.
+    // positions before the product's first tile emit carry 0.
     GP mine{0, 1};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int64_t j = hi - 4 * lane - q;
-      const GP f = j >= 0 ? gp_of(flags[j], bad) : GP{0, 0};
+      const GP f = j >= static_cast<int64_t>(first) ? gp_of(flags[j], bad) : GP{0, 0};
       mine = gp_compose(f, mine);
     }
     if (__any_sync(0xffffffffu, bad)) {
@@ -563,14 +494,14 @@ __global__ void __launch_bounds__(kFixWarps * 32) carry_fix_kernel(uint64_t *out
     }
     const GP win{__shfl_sync(0xffffffffu, mine.g, 0), __shfl_sync(0xffffffffu, mine.p, 0)};
     acc = gp_compose(win, acc);
-    if (!acc.p) break;  // decided: a window reaching past tile 0 always ends here
+    if (!acc.p) break;  // decided: a window that reaches past the first tile always ends here
   }
   const uint32_t cin = acc.g;
   const uint64_t base = t * kCarryTile;
   const uint64_t end = base + kCarryTile < nproc ? base + kCarryTile : nproc;
-  if (t == tiles - 1 && lane == 0 && !drop_top) {
+  if (t == ntiles - 1 && lane == 0 && !drop_top) {
     bool b2 = false;
-    const GP own = gp_of(flags[t], b2);
+    const GP own = gp_of(flags[gt], b2);
     if (own.g | (own.p & cin)) atomicCAS(ss.err, kDevOk, kDevCarryOverflow);
   }
   if (!cin) return;
@@ -590,17 +521,20 @@ __global__ void __launch_bounds__(kFixWarps * 32) carry_fix_kernel(uint64_t *out
   }
 }
 
+// The two launches of a carry over `tiles` tiles (a batch: tpp per product).
 template <class Producer>
-cudaError_t launch_local_carry(const Producer &prod, uint64_t *out, uint64_t nproc, uint64_t tiles, const ScanState &ss,
-                               cudaStream_t st) {
+cudaError_t launch_carry(const Producer &prod, uint64_t *out, uint64_t nproc, uint64_t tiles, const ScanState &ss,
+                         cudaStream_t st, const ProductDesc *batch = nullptr, uint64_t tpp = 0,
+                         uint64_t ws_stride = 0, uint64_t n = 0) {
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  carry_kernel<Producer, true><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, nullptr,
-                                                                                      0, 0, 0);
+  carry_kernel<Producer><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, out, nproc, ss, batch, tpp,
+                                                                                ws_stride, n);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const uint64_t blocks = (tiles + kFixWarps - 1) / kFixWarps;
-  carry_fix_kernel<<<static_cast<unsigned>(blocks), kFixWarps * 32, 0, st>>>(out, nproc, tiles, ss, prod.drop_top());
+  carry_fix_kernel<<<static_cast<unsigned>(blocks), kFixWarps * 32, 0, st>>>(out, nproc, tiles, ss, prod.drop_top(),
+                                                                             batch, tpp, n);
   return cudaGetLastError();
 }
 
@@ -621,7 +555,7 @@ cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, 
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  return launch_local_carry(CrtProducer{res, n, cc}, out, nproc, tiles, ss, st);
+  return launch_carry(CrtProducer{res, n, cc}, out, nproc, tiles, ss, st);
 }
 
 cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int logN, const CrtConst &cc,
@@ -631,10 +565,7 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
   const uint64_t tiles = tpp * nprod;
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  CrtProducer prod{res, n, cc};
-  carry_kernel<CrtProducer, false><<<static_cast<unsigned>(tiles), kCarryThreads, 0, st>>>(prod, nullptr, 0, ss, batch, tpp,
-                                                                                   ws_stride, n);
-  return cudaGetLastError();
+  return launch_carry(CrtProducer{res, n, cc}, nullptr, 0, tiles, ss, st, batch, tpp, ws_stride, n);
 }
 
 cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int logN, uint64_t chunk,
@@ -646,7 +577,7 @@ cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  return launch_local_carry(ChunkProducer{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks}, out, nproc, tiles, ss,
+  return launch_carry(ChunkProducer{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks}, out, nproc, tiles, ss,
                             st);
 }
 
@@ -665,7 +596,7 @@ cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const u
     top_diff_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(a, na, b, nb, n, top);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  cudaError_t e = launch_local_carry(prod, out, nproc, tiles, ss, st);
+  cudaError_t e = launch_carry(prod, out, nproc, tiles, ss, st);
   if (e != cudaSuccess) return e;
   sum_finish_kernel<<<1, 256, 0, st>>>(out, nproc, prod, sa, sb, result);
   return cudaGetLastError();
@@ -684,7 +615,7 @@ cudaError_t launch_schoolboy_carry(const uint64_t *x, uint64_t nx, const uint64_
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  return launch_local_carry(ConvProducer{x, nx, y, ny, 0}, out, nproc, tiles, ss, st);
+  return launch_carry(ConvProducer{x, nx, y, ny, 0}, out, nproc, tiles, ss, st);
 }
 
 cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint64_t *out, uint64_t nout,
@@ -693,7 +624,7 @@ cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint6
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
-  return launch_local_carry(ConvProducer{x, nx, nullptr, 1, d}, out, nproc, tiles, ss, st);
+  return launch_carry(ConvProducer{x, nx, nullptr, 1, d}, out, nproc, tiles, ss, st);
 }
 
 }  // namespace hg

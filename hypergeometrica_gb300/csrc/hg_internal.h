@@ -100,7 +100,7 @@ struct CrtConst {
   uint64_t p01_lo, p01_hi;  // p0 * p1
 };
 
-// Carry-scan launch state (decoupled look-back across tiles).
+// Carry launch state: tile tickets and the tiles' published aggregates.
 struct ScanState {
   unsigned long long *ticket;  // monotonically increasing tile ticket
   unsigned long long ticket_base;

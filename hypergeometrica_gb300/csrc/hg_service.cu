@@ -123,7 +123,6 @@ int slot_alloc(SvcSlot &s, uint64_t ws_bytes, size_t max_batch) {
 }
 
 int err_code(int dev_err) {
-  if (dev_err == kDevTimeout) return HG_ERR_TIMEOUT;
   if (dev_err == kDevCarryOverflow || dev_err == kDevTicket) return HG_ERR_INCONSISTENT;
   return HG_ERR_CUDA;
 }

@@ -46,7 +46,7 @@ extern "C" {
 #define HG_ERR_CUDA (-4)         /* a CUDA runtime call failed                               */
 #define HG_ERR_INCONSISTENT (-5) /* a carry ran past the result storage                      */
                                  /* (add-big-digit, src/ntt-multiply.lisp:19-22)            */
-#define HG_ERR_TIMEOUT (-6)      /* a bounded device wait gave up; results are invalid       */
+#define HG_ERR_TIMEOUT (-6)      /* a bounded wait for the multiply service gave up          */
 #define HG_ERR_NOT_INIT (-7)     /* hg_init failed or was given foreign moduli               */
 
 /* Library initialisation.  Replaces the load-time construction of the
