@@ -137,6 +137,36 @@ def test_batch_edge_products(hg):
         assert int.from_bytes(got.astype("<u8").tobytes(), "little") == want, (nx, ny)
 
 
+def test_batch_all_ones_carries(hg):
+    """(2^(64n) - 1)(2^(64m) - 1): runs of zero limbs that only a carry
+    rippling through whole 4096-limb tiles produces, in products that share a
+    batch with uniform ones (the carry's second launch stops at each
+    product's first tile)."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+
+    ones = W.limbs(0, 20000, "ones")
+    specs = [(5000, 5000), (9000, 4000), (12000, None), (20000, 13000), (3000, 2500)]
+    items, want = [], []
+    for k, (nx, ny) in enumerate(specs):
+        x = ones[:nx]
+        y = None if ny is None else (ones[:ny] if k != 4 else W.limbs(77, ny, "uniform"))
+        nout = (2 * nx if y is None else nx + ny) + 2
+        items.append((_dev(x), None if y is None else _dev(y), torch.full((nout,), -1, dtype=torch.int64,
+                                                                          device="cuda")))
+        xi = int.from_bytes(x.astype("<u8").tobytes(), "little")
+        yi = xi if y is None else int.from_bytes(y.astype("<u8").tobytes(), "little")
+        want.append(xi * yi)
+    D.mul_batch(items)
+    D.sync()
+    for k, it in enumerate(items):
+        got = int.from_bytes(_host(it[2]).astype("<u8").tobytes(), "little")
+        assert got == want[k], specs[k]
+        assert _single(hg, _host(it[0]), None if it[1] is None else _host(it[1]), it[2].numel()).tobytes() == \
+            _host(it[2]).tobytes(), specs[k]
+
+
 def test_graph_capture_before_any_warm_run(hg):
     """A batch captured into a CUDA graph on its first run, for a transform
     length (2^16) no earlier test in this file builds inter-pass tables for,
