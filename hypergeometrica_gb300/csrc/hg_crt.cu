@@ -440,12 +440,12 @@ __global__ void __launch_bounds__(kCarryThreads, kCarryMinBlocks) carry_kernel(c
 // (batch != nullptr) index tiles as the tile launch does.
 //
 // A carry-in of 1 changes only the tile's leading run of positions that
-// propagate.  p at a position means A = 2^64 - 1 with no carry out (A is
-// the position's sum before carries, and a carry out of it leaves at most 1,
-// so A = 2^64 - 1 always propagates), and the tile launch wrote exactly A
-// there: the run is the tile's leading limbs equal to 2^64 - 1.  They become
-// 0 and the first limb after them gains 1; a tile that is one run becomes 0
-// and passes the carry on, as its p = 1 aggregate already says.
+// propagate.  A position propagates exactly when its low word before
+// carries, A, is 2^64 - 1: a position that generates a carry wraps to a low
+// word of at most 1.  The tile launch wrote exactly A at every position of
+// that run, so the run is the tile's leading limbs equal to 2^64 - 1.  They
+// become 0 and the first limb after them gains 1; a tile that is one run
+// becomes 0 and passes the carry on, as its p = 1 aggregate already says.
 constexpr int kFixWarps = 8;
 
 __global__ void __launch_bounds__(kFixWarps * 32)
