@@ -202,30 +202,29 @@ def gmp_baseline(x, y, gpu_out) -> dict:
 
 
 def run_reference(args) -> None:
+    """The reference arm: the oracle port (the reference's algorithm with its
+    per-modulus task structure, src/ntt-multiply.lisp:174-254 under
+    with-parallel-work) timed on this host's cores on the bench's own
+    workload, one full 2^24 x 2^24-limb product per timed step.  Warm-up
+    steps run one 2^20 x 2^20 product each (they only page the code and the
+    thread pool in).  Beside the per-modulus-threaded line, one full product
+    runs single-threaded."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
     cores, model = _cpu_info()
     threads = min(6, cores)  # 2k forward tasks of with-parallel-work (k = 3 primes)
     full = 1 << LOG_SIZE
-    # Size each step so that warm-up + timed steps stay within about 3 minutes.
-    rate20, t20 = cpu_product_rate(20, threads)
-    est_full = t20 * (full / (1 << 20)) * (25 / 21)
-    budget = 180.0 / max(1, args.steps + args.warmup)
-    log_s = LOG_SIZE
-    while log_s > 16 and est_full * (2 ** (log_s - LOG_SIZE)) > budget:
-        log_s -= 1
     for _ in range(args.warmup):
-        cpu_product_rate(log_s, threads)
+        cpu_product_rate(20, threads)
     times = []
     for _ in range(args.steps):
-        _, dt = cpu_product_rate(log_s, threads)
+        _, dt = cpu_product_rate(LOG_SIZE, threads)
         times.append(dt)
     total = sum(times)
-    n_out = 2 * (1 << log_s)
-    value = n_out * args.steps / total
-    sample = (f"one {1 << log_s}x{1 << log_s}-limb product per step" +
-              ("" if log_s == LOG_SIZE else f" (the {full}x{full} workload scaled down to fit the time budget)"))
+    value = 2 * full * args.steps / total
+    rate1, dt1 = cpu_product_rate(LOG_SIZE, 1)
+    sample = f"one {full}x{full}-limb product per timed step (warm-up steps: one 2^20 x 2^20 product each)"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
@@ -233,7 +232,9 @@ def run_reference(args) -> None:
         "config": {"workload": f"mul {full}x{full} limbs, transform 2^{LOG_SIZE + 1}, 3 primes",
                    "dist": "uniform", "parallelism": "replicas"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
-                         "cpu": model, "host_cores": cores},
+                         "cpu": model, "host_cores": cores,
+                         "single_thread": {"value": rate1, "unit": UNIT, "cores": 1,
+                                           "sample": f"one {full}x{full}-limb product ({dt1:.1f} s)"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -379,6 +380,49 @@ def run_batched(stream, steps: int) -> dict:
 
 
 SWEEP_LOG_SIZES = (18, 20, 22, 24, 26)
+UNBALANCED = ((24, 16), (25, 20), (20, 6))
+DISTS = ("uniform", "ones", "sparse")
+
+
+class ExactChecks:
+    """GMP's exact products of the sweep's operands, computed on host threads
+    while the GPU is timed (ctypes releases the interpreter lock inside
+    mpz_mul; four cores stay free for the launching thread).  check() compares
+    a GPU result limb for limb; where libgmp is missing it falls back to the
+    residue modulo 2^31 - 1 and says so."""
+
+    def __init__(self, jobs):
+        import concurrent.futures as cf
+
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import gmp
+
+        self.gmp = gmp if gmp.available() else None
+        self.futs = {}
+        self.ex = None
+        if self.gmp:
+            self.ex = cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), (os.cpu_count() or 5) - 4)))
+            for key, (kind, xs, ys) in sorted(jobs.items(), key=lambda kv: -kv[1][1][1] * (kv[1][2] or kv[1][1])[1]):
+                self.futs[key] = self.ex.submit(self._product, kind, xs, ys)
+
+    def _product(self, kind, xs, ys):
+        from hypergeometrica_gb300 import workloads as W
+
+        x = W.limbs(*xs)
+        return self.gmp.sqr(x) if kind == "sqr" else self.gmp.mul(x, W.limbs(*ys))
+
+    def check(self, key, got, x, y) -> tuple[bool, str]:
+        import numpy as np
+
+        if key in self.futs:
+            want = self.futs[key].result()
+            return bool(len(got) >= len(want) and np.array_equal(got[: len(want)], want)
+                        and not got[len(want):].any()), "gmp limb-exact"
+        return _residue_ok(got, x, y), "residue mod 2^31-1"
+
+    def close(self):
+        if self.ex:
+            self.ex.shutdown(wait=True, cancel_futures=True)
 
 
 def run_sweep(stream, peak_gbs: float) -> dict:
@@ -393,6 +437,14 @@ def run_sweep(stream, peak_gbs: float) -> dict:
     from hypergeometrica_gb300 import device as D
     from hypergeometrica_gb300 import workloads as W
 
+    jobs = {}
+    for k in SWEEP_LOG_SIZES:
+        jobs[("mul", k)] = ("mul", (11, 1 << k, "uniform"), (12, 1 << k, "uniform"))
+        jobs[("sqr", k)] = ("sqr", (11, 1 << k, "uniform"), None)
+    for ka, kb in UNBALANCED:
+        for dist in DISTS:
+            jobs[("unb", ka, kb, dist)] = ("mul", (13, 1 << ka, dist), (14, 1 << kb, dist))
+    exact = ExactChecks(jobs)
     out = {"workload": "a*b and a^2, |a| = |b| = 2^k limbs, uniform", "unit": "limbs/s", "lines": []}
     for k in SWEEP_LOG_SIZES:
         n = 1 << k
@@ -415,10 +467,11 @@ def run_sweep(stream, peak_gbs: float) -> dict:
             ms = ev0.elapsed_time(ev1) / reps
             D.sync(stream)
             x = W.limbs(11, n)
-            ok = _residue_ok(o.cpu().numpy().view(np.uint64), x, x if kind == "sqr" else W.limbs(12, n))
+            ok, how = exact.check((kind, k), o.cpu().numpy().view(np.uint64), x,
+                                  x if kind == "sqr" else W.limbs(12, n))
             algo = (16 * 2 * n + 192 * N) if kind == "mul" else (24 * n + 96 * N)
             out["lines"].append({"log_size": k, "kind": kind, "ms": ms, "limbs_per_s": 2 * n / (ms / 1000.0),
-                                 "hbm_frac": algo / (ms / 1000.0) / 1e9 / peak_gbs, "correct": ok})
+                                 "hbm_frac": algo / (ms / 1000.0) / 1e9 / peak_gbs, "correct": ok, "check": how})
         del a, b, o
         torch.cuda.empty_cache()
     # Unbalanced and edge-value products: 2^24 x 2^16, 2^25 x 2^20, 2^20 x 2^6
@@ -430,9 +483,9 @@ def run_sweep(stream, peak_gbs: float) -> dict:
     from hypergeometrica_gb300 import _lib
 
     out["unbalanced"] = []
-    for ka, kb in ((24, 16), (25, 20), (20, 6)):
+    for ka, kb in UNBALANCED:
         na, nb = 1 << ka, 1 << kb
-        for dist in ("uniform", "ones", "sparse"):
+        for dist in DISTS:
             xh, yh = W.limbs(13, na, dist), W.limbs(14, nb, dist)
             a = torch.from_numpy(xh.view(np.int64)).cuda()
             b = torch.from_numpy(yh.view(np.int64)).cuda()
@@ -459,13 +512,15 @@ def run_sweep(stream, peak_gbs: float) -> dict:
                 ms1 = timed(o1)
             finally:
                 _lib.set_chunking(True)
-            ok = _residue_ok(o.cpu().numpy().view(np.uint64), xh, yh) and bool(torch.equal(o, o1))
+            ok, how = exact.check(("unb", ka, kb, dist), o.cpu().numpy().view(np.uint64), xh, yh)
+            ok = ok and bool(torch.equal(o, o1))
             out["unbalanced"].append({"log_sizes": [ka, kb], "dist": dist, "ms": ms,
                                       "limbs_per_s": (na + nb) / (ms / 1000.0),
                                       "chunk_plan": _lib.chunk_plan(na, nb), "ms_one_transform": ms1,
-                                      "correct": ok})
+                                      "correct": ok, "check": how + "; chunked equals one transform"})
             del a, b, o, o1
         torch.cuda.empty_cache()
+    exact.close()
     out["correct"] = all(line["correct"] for line in out["lines"] + out["unbalanced"])
     return out
 

@@ -78,6 +78,7 @@ class HgSvcStats(ctypes.Structure):
 # name -> (restype, argtypes)
 SIGNATURES = {
     "hg_init": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int]),
+    "hg_init_scheme": (ctypes.c_int, [_u64p, ctypes.c_int, _u64p, ctypes.c_int, ctypes.c_int]),
     "hg_shutdown": (ctypes.c_int, []),
     "hg_last_error": (ctypes.c_int, [ctypes.c_char_p, _sz]),
     "hg_scheme_moduli": (ctypes.c_int, [_u64p, ctypes.c_int]),

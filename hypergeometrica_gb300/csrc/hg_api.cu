@@ -222,7 +222,43 @@ uint32_t swz_tw_h(uint32_t e) { return e ^ ((e >> 3) & 7u) ^ ((e >> 6) & 7u) ^ (
 // Shoup companion floor(w * 2^64 / p) (calc-b-inv, src/modular-arithmetic.lisp:207-208).
 uint64_t shoup_h(uint64_t w, uint64_t p) { return static_cast<uint64_t>(((u128)w << 64) / p); }
 
-int init_locked(const uint64_t *moduli, int k, int device) {
+// Largest transform the reference's scheme supports for these moduli
+// (max-transform-length-bits, src/moduli.lisp:266-267): every p - 1 is
+// divisible by 2^55.
+constexpr int kSchemeMaxLg = 55;
+
+// A caller's table of primitive roots against the library's: roots[i *
+// (maxlg + 1) + q] must be w_{2^q} for moduli[i], the root the scheme's
+// table holds at [q][i][0][0] (find-primitive-root of 2^q, the generator
+// raised to (m - 1) / 2^q, src/moduli.lisp:181-191, 318-332).  For q <= 30
+// the library's device tables are built from w_{2^30}, so the expected root
+// is w_{2^30}^(2^(30 - q)), the very value they use; above 30 it is the
+// generator's power.
+int check_roots(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg) {
+  if (!roots) return HG_OK;
+  if (!moduli || k <= 0) return fail(HG_ERR_NOT_INIT, "a roots table needs the moduli it belongs to");
+  if (maxlg < 0 || maxlg > kSchemeMaxLg)
+    return fail(HG_ERR_NOT_INIT, "roots table of 2^0 .. 2^%d: the scheme's transforms stop at 2^%d", maxlg,
+                kSchemeMaxLg);
+  for (int i = 0; i < k; ++i) {
+    const uint64_t m = moduli[i];
+    const uint64_t g = generator_h(m);
+    const uint64_t w30 = powmod_h(g, (m - 1) >> kLogNmax, m);
+    for (int q = 0; q <= maxlg; ++q) {
+      const uint64_t want = q <= kLogNmax ? powmod_h(w30, uint64_t(1) << (kLogNmax - q), m)
+                                          : powmod_h(g, (m - 1) >> q, m);
+      const uint64_t got = roots[static_cast<size_t>(i) * (maxlg + 1) + q];
+      if (got != want)
+        return fail(HG_ERR_NOT_INIT,
+                    "primitive 2^%d-th root of unity for modulus %d (0x%llx) is 0x%llx in the caller's scheme, 0x%llx "
+                    "in the library's tables",
+                    q, i, (unsigned long long)m, (unsigned long long)got, (unsigned long long)want);
+    }
+  }
+  return HG_OK;
+}
+
+int init_locked(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg, int device) {
   Context &c = g_ctx;
   std::vector<uint64_t> dm = default_moduli_h();
   if (dm.size() != kPrimes) return fail(HG_ERR_NOT_INIT, "expected %d default moduli, found %zu", kPrimes, dm.size());
@@ -232,6 +268,8 @@ int init_locked(const uint64_t *moduli, int k, int device) {
     if (given != dm)
       return fail(HG_ERR_NOT_INIT, "moduli differ from the scheme this library implements (default-moduli)");
   }
+  int rc = check_roots(moduli, k, roots, maxlg);
+  if (rc) return rc;
   if (c.ready) {
     if (device >= 0 && device != c.device)
       return fail(HG_ERR_ARG, "library already initialised on device %d", c.device);
@@ -318,7 +356,7 @@ int init_locked(const uint64_t *moduli, int k, int device) {
 
 int ensure_init() {
   if (g_ctx.ready) return HG_OK;
-  return init_locked(nullptr, 0, -1);
+  return init_locked(nullptr, 0, nullptr, 0, -1);
 }
 
 int ilog2_ceil(uint64_t n) {
@@ -1449,7 +1487,12 @@ int hg_mul_batch_device(const hg_product *prods, size_t n, void *stream) {
 
 int hg_init(const uint64_t *moduli, int k, int device) {
   std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
-  return init_locked(moduli, k, device);
+  return init_locked(moduli, k, nullptr, 0, device);
+}
+
+int hg_init_scheme(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg, int device) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  return init_locked(moduli, k, roots, maxlg, device);
 }
 
 int hg_shutdown(void) {
@@ -1482,6 +1525,10 @@ int hg_shutdown(void) {
   c.copy_done = nullptr;
   c.ws_pending = false;
   c.ready = false;
+  // The scratch array's device address belongs to the module as loaded in
+  // the current context: after a context reset the module loads again, so
+  // the next hg_mul_device_noalloc looks the address up afresh.
+  for (uint64_t *&p : g_noalloc_ptr) p = nullptr;
   return HG_OK;
 }
 

@@ -58,6 +58,16 @@ extern "C" {
  * first entry point when not called explicitly. */
 int hg_init(const uint64_t *moduli, int k, int device);
 
+/* hg_init that also checks the caller's table of primitive roots against the
+ * library's (make-modular-scheme's primitive-roots, src/moduli.lisp:302-353):
+ * roots[i * (maxlg + 1) + q] is w_{2^q}, the primitive 2^q-th root of unity
+ * modulo moduli[i] (the Lisp table's entry [q][i][0][0]), for q = 0 .. maxlg,
+ * maxlg <= 55.  A scheme built with another generator would give other
+ * spectra; any root that differs from the one the library's device tables
+ * are built from fails with HG_ERR_NOT_INIT before anything is allocated.
+ * roots may be NULL (then this is hg_init). */
+int hg_init_scheme(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg, int device);
+
 /* Release every device buffer, stream and table held by the library. */
 int hg_shutdown(void);
 
@@ -154,7 +164,13 @@ int hg_mul_schoolboy_device(const uint64_t *x, size_t nx, const uint64_t *y, siz
  *    between them, or several host threads) race and corrupt each other's
  *    results.  Issue them on one stream, or order them with events.
  *    hg_mul_device and the batch API use other storage and do not race
- *    with it. */
+ *    with it.
+ *  - Errors found on the device (a carry out of the top of out, which no
+ *    exact product causes) latch the library's device error word, which the
+ *    next hg_sync reports; the call itself reports only host-side errors.
+ *  - hg_shutdown forgets the scratch address: after a reset of the device's
+ *    context, call hg_shutdown and hg_init around it, and the next call looks
+ *    the address up again. */
 int hg_mul_device_noalloc(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout,
                           void *stream);
 

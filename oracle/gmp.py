@@ -83,6 +83,27 @@ def mul(x: np.ndarray, y: np.ndarray, timer=None) -> np.ndarray:
     return out[: len(x) + len(y)]
 
 
+def sqr(x: np.ndarray, timer=None) -> np.ndarray:
+    """x * x through mpz_mul with one operand passed twice (GMP then squares):
+    2 len(x) limbs.  With `timer` (a list), the seconds spent in mpz_mul are
+    appended."""
+    import time
+
+    g = _load()
+    zx, zr = _from_limbs(g, x), _MPZ()
+    g.__gmpz_init(ctypes.byref(zr))
+    t = time.perf_counter()
+    g.__gmpz_mul(ctypes.byref(zr), ctypes.byref(zx), ctypes.byref(zx))
+    if timer is not None:
+        timer.append(time.perf_counter() - t)
+    out = _export(g, zr, 2 * len(x) + 1)
+    for z in (zx, zr):
+        g.__gmpz_clear(ctypes.byref(z))
+    full = np.zeros(2 * len(x), dtype=np.uint64)
+    full[: len(out)] = out
+    return full
+
+
 def _export(g, z: _MPZ, nlimbs: int) -> np.ndarray:
     out = np.zeros(nlimbs, dtype=np.uint64)
     cnt = ctypes.c_size_t(0)

@@ -93,3 +93,47 @@ def test_no_cpu_fallback_without_gpu(lib):
     a = np.ones(4, dtype=np.uint64)
     out = np.zeros(8, dtype=np.uint64)
     assert lib.hg_mul(a.ctypes.data, 4, a.ctypes.data, 4, out.ctypes.data, 8) != 0
+
+
+def _scheme_roots(oracle, maxlg):
+    """w_{2^q} for every modulus, q = 0 .. maxlg, from the oracle's restated
+    make-modular-scheme (the Lisp table's [q][i][0][0])."""
+    s = oracle.scheme()
+    L = oracle.lib()
+    return [[int(L.hgo_scheme_root(s, q, i, 0, 0)) for q in range(maxlg + 1)] for i in range(3)]
+
+
+def _init_scheme(lib, moduli, roots, maxlg):
+    from hypergeometrica_gb300 import _lib
+
+    m = (ctypes.c_uint64 * 3)(*moduli)
+    flat = [w for row in roots for w in row]
+    r = (ctypes.c_uint64 * len(flat))(*flat)
+    rc = lib.hg_init_scheme(m, 3, r, maxlg, -1)
+    return rc, _lib.last_error()
+
+
+def test_init_checks_scheme_roots(lib, oracle):
+    """hg_init_scheme accepts the reference's own roots table and rejects a
+    perturbed one, or one past the scheme's 2^55 limit, with HG_ERR_NOT_INIT
+    before touching the device (src/moduli.lisp:302-353)."""
+    from hypergeometrica_gb300 import _lib
+
+    moduli = oracle.moduli()
+    good = _scheme_roots(oracle, 55)
+    rc, _ = _init_scheme(lib, moduli, good, 55)
+    assert rc in (_lib.HG_OK, _lib.HG_ERR_CUDA)  # HG_ERR_CUDA: no GPU in this process
+    rc, _ = _init_scheme(lib, moduli, [row[:31] for row in good], 30)
+    assert rc in (_lib.HG_OK, _lib.HG_ERR_CUDA)
+    for i, q in ((0, 30), (1, 7), (2, 55), (0, 1)):
+        bad = [row[:] for row in good]
+        bad[i][q] = (bad[i][q] * 3) % moduli[i]
+        rc, msg = _init_scheme(lib, moduli, bad, 55)
+        assert rc == _lib.HG_ERR_NOT_INIT and f"2^{q}-th root" in msg, (i, q, msg)
+    # roots of another generator: w_{2^q} = 5^((m - 1) / 2^q) is not the scheme's for modulus 0
+    other = [row[:] for row in good]
+    other[0] = [pow(5, (moduli[0] - 1) >> q, moduli[0]) for q in range(56)]
+    rc, _ = _init_scheme(lib, moduli, other, 55)
+    assert rc == _lib.HG_ERR_NOT_INIT
+    rc, msg = _init_scheme(lib, moduli, [row + [1] for row in good], 56)
+    assert rc == _lib.HG_ERR_NOT_INIT and "2^55" in msg

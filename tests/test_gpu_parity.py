@@ -208,6 +208,50 @@ def test_mpz_dispatch_vs_oracle(hg, oracle):
         assert got.sign == s and np.array_equal(got.storage, mag)
 
 
+@pytest.mark.parametrize("n", [2, 7, 64, 100, 101, 160])
+def test_mpz_dispatch_same_object_threshold(hg, oracle, n):
+    """(eq x y) below the threshold goes to schoolboy, not to mpz-square: the
+    threshold test comes first in mpz-* (src/multiply.lisp:37-44).  The
+    schoolboy storage (1 + 2n digits before optimize-mpz) and mpz-square's
+    (a power of two) both trim to the same magnitude, so the branch is
+    checked through the C ABI's dispatch as well, whose result size is the
+    trimmed size either way, and through the storage the host mirror
+    returns."""
+    import ctypes
+
+    from hypergeometrica_gb300 import _lib
+
+    a = W.limbs(500 + n, n, "uniform")
+    for thr in (100, 1 << 40, 0):
+        x = hg.MPZ(-1, a.copy())
+        got = hg.mpz_mul(x, x, threshold=thr)
+        mag, s = oracle.mpz_mul(a, -1, a, -1, True, thr)
+        assert got.sign == s == 1 and np.array_equal(got.storage, mag), (n, thr)
+        out = np.zeros(2 * n + 1 if n <= thr else int(_lib.load().hg_ntt_length(n, n)), dtype=np.uint64)
+        nres, sres = ctypes.c_size_t(0), ctypes.c_int(0)
+        _lib.check(_lib.load().hg_mpz_mul(a.ctypes.data, n, -1, a.ctypes.data, n, -1, 1, thr, out.ctypes.data,
+                                          len(out), ctypes.byref(nres), ctypes.byref(sres)))
+        assert sres.value == 1 and np.array_equal(out[: nres.value], mag), (n, thr)
+
+
+def test_mpz_dispatch_branch_taken(hg, monkeypatch):
+    """Which branch mpz-* takes for (eq x y): schoolboy when size <= the
+    threshold, mpz-square above it (src/multiply.lisp:37-44)."""
+    from hypergeometrica_gb300 import mpz as M
+
+    taken = []
+    real_school, real_square = M.multiply_storage_schoolboy, M.mpz_square
+    monkeypatch.setattr(M, "multiply_storage_schoolboy",
+                        lambda *a: taken.append("schoolboy") or real_school(*a))
+    monkeypatch.setattr(M, "mpz_square", lambda *a: taken.append("square") or real_square(*a))
+    for n, thr, want in ((100, 100, "schoolboy"), (101, 100, "square"), (5, 4, "square"), (5, 5, "schoolboy")):
+        taken.clear()
+        x = hg.MPZ(1, W.limbs(900 + n, n, "uniform"))
+        r = M.mpz_mul(x, x, threshold=thr)
+        assert taken == [want], (n, thr, taken)
+        assert r.to_int() == x.to_int() ** 2
+
+
 def test_small_paths_vs_oracle(hg, oracle):
     x = W.limbs(1, 5000, "uniform")
     y = W.limbs(2, 100, "uniform")

@@ -197,3 +197,41 @@ def test_records_submission_and_shutdown_guard(hg):
         svc.close()
     for k, (_, _, out) in enumerate(items):
         assert np.array_equal(_host(out), want[k]), k
+
+
+def test_bounded_waits_time_out_then_finish(hg):
+    """hg_svc_wait and hg_svc_wait_all give up with HG_ERR_TIMEOUT when their
+    limit runs out before the products finish; the products still finish,
+    and a later wait without a limit returns them complete and exact.  The
+    limit runs out on the host: nothing on the GPU is made to wait."""
+    from hypergeometrica_gb300 import device as D
+    from hypergeometrica_gb300._lib import HG_ERR_TIMEOUT, HGError
+
+    n = 1 << 22
+    items = []
+    for k in range(3):
+        x = _dev(W.limbs(600 + 2 * k, n))
+        y = _dev(W.limbs(601 + 2 * k, n))
+        items.append((x, y, _full(2 * n)))
+    _sync()
+    want = _alone(items)
+    for _, _, out in items:
+        out.fill_(-1)
+    _sync()
+    # one 2^23-point product at a time per slot: several milliseconds each
+    with D.Service(workspace_bytes=2 * 420 << 20, slots=1, max_batch=1) as svc:
+        tickets = svc.submit(items)
+        with pytest.raises(HGError) as e:
+            svc.wait(tickets[-1], timeout=1e-6)
+        assert e.value.code == HG_ERR_TIMEOUT and "not finished" in str(e.value)
+        with pytest.raises(HGError) as e:
+            svc.wait_all(timeout=1e-6)
+        assert e.value.code == HG_ERR_TIMEOUT
+        assert svc.status(tickets[-1]) == 0  # still pending or running
+        svc.wait(tickets[-1])
+        svc.wait_all(timeout=120)
+        assert all(svc.status(t) == 1 for t in tickets)
+        st = svc.stats()
+    assert st["completed"] == 3 and st["failed"] == 0
+    for k, (_, _, out) in enumerate(items):
+        assert np.array_equal(_host(out), want[k]), k
