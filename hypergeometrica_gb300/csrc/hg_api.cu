@@ -409,6 +409,7 @@ PassArgs base_args(int L, int nops) {
     a.pc[i] = g_ctx.pc[i];
     a.tb[i] = g_ctx.tb[i];
   }
+  a.err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
   return a;
 }
 
@@ -990,6 +991,7 @@ int read_device_error(cudaStream_t st) {
     HG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st), "error word reset");
     HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
     if (err == kDevCarryOverflow) return fail(HG_ERR_INCONSISTENT, "a carry left the top of the result storage");
+    if (err == kDevCopyTimeout) return fail(HG_ERR_CUDA, "a tile copy did not complete within its wait limit");
     return fail(HG_ERR_CUDA, "device error %d", err);
   }
   return HG_OK;
@@ -1174,6 +1176,7 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   uint64_t *ws = bb.ws;
   if (g.tails) HG_CUDA(launch_zero_tails(d, g.nprod, N, st), "zero tails");
   PassArgs a = base_args(g.L, nops);
+  a.err = bb.err;
   a.batch = d;
   a.read_limbs = 1;
   a.nprod = g.nprod;
@@ -1185,6 +1188,7 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   if (plan.size() > 1) m.read_limbs = 0;
   HG_CUDA(run_contig(m, plan.back(), g.square ? kContigSqr : kContigMul, st), "middle pass");
   PassArgs inv = base_args(g.L, 1);
+  inv.err = bb.err;
   inv.batch = d;
   inv.nprod = g.nprod;
   inv.ws_stride = slab;

@@ -36,7 +36,13 @@ enum DevErr : int {
   kDevOk = 0,
   kDevCarryOverflow = 2,  // a carry left the top of the result
   kDevTicket = 3,         // a carry tile ticket fell outside its launch, or a tile aggregate of another launch
+  kDevCopyTimeout = 4,    // a tile copy (TMA) did not land within its wait limit
 };
+
+// Latch `code` in the device error word (the first error wins).
+__device__ __forceinline__ void latch_error(int *err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
 
 // x - p when x >= p, else x.  The butterflies' corrections select rather
 // than add a sign mask (17.5 against 19.3 ALU-pipe instructions per forward

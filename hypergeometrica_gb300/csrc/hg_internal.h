@@ -70,6 +70,7 @@ struct PassArgs {
   // (M, R, direction), Montgomery form, [prime][r][s] with M words per prime
   // (all primes of the scheme), or null to form them from tb.
   const uint64_t *ptw;
+  int *err;                    // device error word (a tile copy that did not land)
 };
 
 // Limbs a pass reads for (product, operand), or nullptr when it reads residues.

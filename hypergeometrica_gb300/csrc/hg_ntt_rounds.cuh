@@ -74,10 +74,16 @@ __device__ __forceinline__ uint64_t table_twiddle(uint64_t E, int logM, const ui
 // neighbour is a Montgomery product: forward, it is the last stage and its
 // u + v, u - v + p go uncorrected ([0, 2p)) into the inter-pass twiddle;
 // inverse, it is the first stage and its inputs are already in [0, p).
-template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO, bool EDGE = false>
+//
+// ZTOP (forward only) marks a first stage whose upper inputs are all zero
+// (the zero padding above an operand's limbs): u + 0 and (u - 0) w need
+// neither the sum's correction nor the difference, only the product.
+template <int NB, int JG, int A, int ROWOFF, int BLO, int LOGR, bool INV, bool TZERO, bool EDGE = false,
+          bool ZTOP = false>
 __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__restrict__ tw, uint32_t xt, uint64_t p,
                                        uint32_t c) {
   static_assert(!EDGE || (TZERO && BLO == 0), "the edge stage is the twiddle-free stage on row bit 0");
+  static_assert(!ZTOP || !INV, "zero upper inputs only in a forward pass");
 #pragma unroll
   for (int s = 0; s < NB; ++s) {
     const int jj = INV ? s : NB - 1 - s;
@@ -95,6 +101,15 @@ __device__ __forceinline__ void stages(uint64_t (&v)[16], const ulonglong2 *__re
       if (EDGE && jj == 0) {  // twiddle 1, inputs in [0, p): outputs in [0, 2p)
         v[i] = u + w;
         v[i | (1 << j)] = u - w + p;
+        continue;
+      }
+      if (ZTOP && s == 0) {  // w = 0: v[i] keeps u
+        if (trivial) {
+          v[i | (1 << j)] = u;
+        } else {
+          const ulonglong2 t = tw[ts ^ swz_tw(rp << sh)];
+          v[i | (1 << j)] = shoup_mul(u, t.x, t.y, p, c);
+        }
         continue;
       }
       if (!INV) {
