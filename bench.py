@@ -629,6 +629,50 @@ def _int_roofline(N: int, ms_per_product: float) -> dict:
             "peak_source": "hg_butterfly_peak (register-only network of the same butterflies)"}
 
 
+def host_link(nbytes: int = 256 << 20) -> dict:
+    """Where the pinned buffers sit and what the host link moves: the NUMA
+    nodes of this host, the GPU's node (sysfs), and plain pinned-memory copy
+    rates host->device and device->host (torch copies, CUDA events)."""
+    import glob
+
+    import torch
+
+    info = {"numa_nodes": len(glob.glob("/sys/devices/system/node/node[0-9]*"))}
+    node = None
+    for d in glob.glob("/sys/bus/pci/devices/*"):
+        try:
+            if open(os.path.join(d, "vendor")).read().strip() == "0x10de" and \
+                    open(os.path.join(d, "class")).read().startswith("0x030"):
+                node = int(open(os.path.join(d, "numa_node")).read())
+                break
+        except OSError:
+            continue
+    info["gpu_numa_node"] = node
+    try:
+        info["process_mems_allowed"] = [ln.split(":", 1)[1].strip() for ln in open("/proc/self/status")
+                                        if ln.startswith("Mems_allowed_list")][0]
+    except (OSError, IndexError):
+        pass
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+
+    def rate(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return 5 * nbytes / (e0.elapsed_time(e1) / 1000.0) / 1e9
+
+    info["h2d_gbs"] = rate(lambda: d.copy_(h, non_blocking=True))
+    info["d2h_gbs"] = rate(lambda: h.copy_(d, non_blocking=True))
+    info["copy_bytes"] = nbytes
+    return info
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -707,6 +751,7 @@ def run_ours(args) -> None:
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     clocks = sampler.stop()
     ok = ok and bool(np.array_equal(hout.numpy().view(np.uint64), out.cpu().numpy().view(np.uint64)))
+    link = host_link()
 
     n_out = na + nb
     value = job_rate(ws, n_out, args.steps, ms / 1000.0)
@@ -731,7 +776,8 @@ def run_ours(args) -> None:
         "correct": ok,
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (na + nb),
-                "d2h_bytes_per_step": 8 * n_out, "api": "hg_mul (host pointers, pinned)", "steps": e2e_steps},
+                "d2h_bytes_per_step": 8 * n_out, "api": "hg_mul (host pointers, pinned)", "steps": e2e_steps,
+                "host_link": link},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": d["bytes"] / max(1, d["launches"]),
