@@ -327,6 +327,21 @@ def run_batched(stream, steps: int) -> dict:
     torch.cuda.synchronize()
     D.sync(stream)
     correct = bool(torch.equal(out_b, out_pp))
+    schedule, sched_launches = b.schedule()
+    # Both schedules with the tuned pass splits, each captured in a graph.
+    per_sched = {}
+    for name in ("persistent", "per_pass"):
+        bs = D.Batch(items, autotune=False, schedule=name)
+        gs = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gs, stream=s):
+            bs.run(s)
+        out_b.fill_(-1)
+        gs.replay()
+        torch.cuda.synchronize()
+        D.sync(stream)
+        per_sched[name] = {"graph": gs, "batch": bs, "launches": bs.schedule()[1],
+                           "correct": bool(torch.equal(out_b, out_pp))}
+        correct = correct and per_sched[name]["correct"]
 
     def timed(fn, reps):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -340,6 +355,8 @@ def run_batched(stream, steps: int) -> dict:
 
     with torch.cuda.stream(stream):
         ms_graph = timed(g.replay, max(3, steps))
+        for name, v in per_sched.items():
+            v["ms"] = timed(v["graph"].replay, max(3, steps))
     ms_pp = timed(per_product, max(2, min(steps, 5)))
     D.sync(stream)
 
@@ -375,6 +392,9 @@ def run_batched(stream, steps: int) -> dict:
         "graph": BATCH_PAIRS / (ms_graph / 1000.0), "per_product": BATCH_PAIRS / (ms_pp / 1000.0),
         "speedup": ms_pp / ms_graph, "ms_graph": ms_graph, "ms_per_product_path": ms_pp,
         "gpu_launches_graph": launches_batch, "gpu_launches_per_product_path": launches_pp,
+        "schedule": schedule, "schedule_launches": sched_launches,
+        "schedules": {name: {"ms_graph": v["ms"], "launches": v["launches"], "correct": v["correct"]}
+                      for name, v in per_sched.items()},
         "autotune_s": tune_s, "service": svc_stats, "correct": correct and svc_ok,
     }
 

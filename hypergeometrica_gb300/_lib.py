@@ -56,6 +56,8 @@ class HgProduct(ctypes.Structure):
 
 
 HG_BATCH_AUTOTUNE = 1
+HG_BATCH_PER_PASS = 2
+HG_BATCH_PERSISTENT = 4
 
 
 class HgPoly(ctypes.Structure):
@@ -99,6 +101,7 @@ SIGNATURES = {
     "hg_batch_create": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, ctypes.c_int, ctypes.POINTER(_vp)]),
     "hg_batch_run": (ctypes.c_int, [_vp, _vp]),
     "hg_batch_destroy": (ctypes.c_int, [_vp]),
+    "hg_batch_schedule": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_sz)]),
     "hg_mul_batch_device": (ctypes.c_int, [ctypes.POINTER(HgProduct), _sz, _vp]),
     "hg_add_batch_device": (ctypes.c_int, [_vp, _sz, _vp, _vp]),
     "hg_trim_batch_device": (ctypes.c_int, [_vp, _sz, _vp, _vp]),
@@ -137,7 +140,7 @@ def set_chunking(on: bool) -> bool:
     return bool(load().hg_set_chunking(1 if on else 0))
 
 
-KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "middle", "carry", "small", "other"]
+KERNEL_CLASSES = ["ntt_forward", "ntt_inverse", "middle", "carry", "small", "other", "batch"]
 
 
 def profile_enable(on: bool) -> None:

@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhg_gb300.so")
 
-SOURCES = ["hg_ntt_strided.cu", "hg_ntt_contig.cu", "hg_crt.cu", "hg_api.cu", "hg_service.cu", "hg_sum.cu", "hg_series.cu", "hg_peak.cu"]
+SOURCES = ["hg_ntt_strided.cu", "hg_ntt_contig.cu", "hg_crt.cu", "hg_api.cu", "hg_service.cu", "hg_sum.cu", "hg_series.cu", "hg_peak.cu", "hg_persist.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -1160,6 +1160,12 @@ std::map<std::tuple<int, bool, uint64_t>, std::vector<PassPlan>> g_tuned;
 struct hg_batch {
   hg::BatchPlan bp;
   hg::DevBuf d_desc, ws, flags, tickets;
+  // The persistent schedule: its work list and its counters.
+  std::vector<hg::PersistPhase> phases;
+  uint64_t items = 0;
+  uint64_t persist_flag_words = 0;
+  hg::DevBuf d_phases, d_state;
+  bool persistent = false;
 };
 
 namespace hg {
@@ -1207,16 +1213,221 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   return HG_OK;
 }
 
-int batch_clear_scan(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) {
-  if (bp.flag_words) HG_CUDA(cudaMemsetAsync(bb.flags, 0, bp.flag_words * 8, st), "scan flags reset");
-  if (!bp.groups.empty()) HG_CUDA(cudaMemsetAsync(bb.tickets, 0, bp.groups.size() * 8, st), "scan tickets reset");
-  return HG_OK;
-}
-
 BatchBufs batch_bufs(hg_batch *b) {
   return BatchBufs{static_cast<const ProductDesc *>(b->d_desc.p), b->ws.u64(),
                    static_cast<unsigned long long *>(b->flags.p), static_cast<unsigned long long *>(b->tickets.p),
                    reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8)};
+}
+
+// ---- the persistent schedule (hg_persist.cu) -------------------------------
+//
+// Group workspaces and carry flags lie back to back (the groups run at the
+// same time); the phases of each group follow run_group's launches one for
+// one, with the same arguments.
+constexpr uint64_t kPersistWorkspaceCap = uint64_t(16) << 30;  // bytes
+
+struct PersistLayout {
+  std::vector<uint64_t> ws_off, flag_off;  // per group, words
+  uint64_t ws_words = 0, flag_words = 0;
+};
+
+PersistLayout persist_layout(const BatchPlan &bp) {
+  PersistLayout l;
+  for (const BatchGroup &g : bp.groups) {
+    const uint64_t N = uint64_t(1) << g.L;
+    l.ws_off.push_back(l.ws_words);
+    l.flag_off.push_back(l.flag_words);
+    l.ws_words += static_cast<uint64_t>(g.square ? 1 : 2) * kPrimes * N * g.nprod;
+    l.flag_words += persist_carry_tiles(N) * g.nprod;
+  }
+  return l;
+}
+
+// The phases of one group, in dependency order.
+std::vector<PersistPhase> group_phases(const BatchGroup &g, const BatchBufs &bb, uint64_t *ws,
+                                       unsigned long long *flags, cudaStream_t st) {
+  std::vector<PersistPhase> v;
+  const int nops = g.square ? 1 : 2;
+  const uint64_t N = uint64_t(1) << g.L;
+  const uint64_t slab = static_cast<uint64_t>(kPrimes) * N;
+  const ProductDesc *d = bb.desc + g.first;
+  const std::vector<PassPlan> &plan = g.plan;
+  const int np = static_cast<int>(plan.size()) - 1;
+  auto phase = [](int kind, int sel, uint64_t count) {
+    PersistPhase p{};
+    p.kind = kind;
+    p.sel = sel;
+    p.count = count;
+    p.dep = -1;
+    return p;
+  };
+  PassArgs a = base_args(g.L, nops);
+  a.err = bb.err;
+  a.batch = d;
+  a.read_limbs = 1;
+  a.nprod = g.nprod;
+  a.ws_stride = slab;
+  a.data[0] = ws;
+  a.data[1] = ws + g.nprod * slab;
+  for (int s = 0; s < np; ++s) {
+    PassArgs f = a;
+    f.logR = plan[s].logR;
+    f.logS = plan[s].logS;
+    f.logT = plan[s].logT;
+    f.tiles = N >> plan[s].logT;
+    f.ptw = pass_twiddles(f.logR + f.logS, f.logR, false, st);
+    PersistPhase p = phase(kPhaseStrided, f.logR, f.tiles * g.nprod * static_cast<uint64_t>(nops) * kPrimes);
+    p.a = f;
+    v.push_back(p);
+    a.read_limbs = 0;
+  }
+  {
+    PassArgs m = a;
+    const int T = plan.back().logT;
+    m.logR = T;
+    m.logS = 0;
+    m.logT = T;
+    m.tiles = N >> T;
+    const int mode = g.square ? kContigSqr : kContigMul;
+    if (T < 4) {
+      PersistPhase p = phase(kPhaseTiny, mode, (g.nprod * kPrimes + 255) / 256);
+      p.a = m;
+      v.push_back(p);
+    } else {
+      const uint64_t bpc = uint64_t(1) << (kTileBits - T);
+      const uint64_t gx = (m.tiles * g.nprod + bpc - 1) / bpc;
+      PersistPhase p = phase(kPhaseContig, T | (mode << 4), gx * kPrimes);
+      p.gx = gx;
+      p.a = m;
+      v.push_back(p);
+    }
+  }
+  PassArgs inv = base_args(g.L, 1);
+  inv.err = bb.err;
+  inv.batch = d;
+  inv.nprod = g.nprod;
+  inv.ws_stride = slab;
+  inv.data[0] = ws;
+  for (int s = 0; s < np; ++s) {
+    const PassPlan &pp = plan[np - 1 - s];
+    PassArgs f = inv;
+    f.logR = pp.logR;
+    f.logS = pp.logS;
+    f.logT = pp.logT;
+    f.tiles = N >> pp.logT;
+    f.ptw = pass_twiddles(f.logR + f.logS, f.logR, true, st);
+    PersistPhase p = phase(kPhaseStrided, f.logR | 16, f.tiles * g.nprod * kPrimes);
+    p.a = f;
+    v.push_back(p);
+  }
+  PersistPhase c = phase(kPhaseCarry, 0, persist_carry_tiles(N) * g.nprod);
+  c.res = ws;
+  c.n = N;
+  c.ws_stride = slab;
+  c.cc = crt_const(g.L);
+  c.batch = d;
+  c.tpp = persist_carry_tiles(N);
+  c.tiles = c.tpp * g.nprod;
+  c.ss.ticket = nullptr;
+  c.ss.ticket_base = 0;
+  c.ss.flags = flags;
+  c.ss.epoch = 1;
+  c.ss.err = bb.err;
+  v.push_back(c);
+  PersistPhase f = c;
+  f.kind = kPhaseFix;
+  f.count = (c.tiles + 7) / 8;
+  v.push_back(f);
+  return v;
+}
+
+// Build the work list for the groups' current plans, or leave the batch on
+// the per-pass schedule when it cannot run persistently (too many phases,
+// or group workspaces that together exceed the cap).
+int persist_build(hg_batch *b) {
+  b->phases.clear();
+  b->items = 0;
+  const BatchPlan &bp = b->bp;
+  if (bp.groups.empty() || !persist_grid()) return HG_OK;
+  const PersistLayout l = persist_layout(bp);
+  if (l.ws_words * 8 > kPersistWorkspaceCap) return HG_OK;
+  if (b->ws.bytes < l.ws_words * 8) HG_CUDA(b->ws.ensure(l.ws_words * 8), "batch workspace");
+  if (b->flags.bytes < l.flag_words * 8) HG_CUDA(b->flags.ensure(l.flag_words * 8), "batch scan flags");
+  b->persist_flag_words = l.flag_words;
+  const BatchBufs bb = batch_bufs(b);
+  std::vector<std::vector<PersistPhase>> per;
+  std::vector<PersistPhase> indep;  // zeroing: waits for nothing
+  for (size_t gi = 0; gi < bp.groups.size(); ++gi) {
+    const BatchGroup &g = bp.groups[gi];
+    per.push_back(group_phases(g, bb, bb.ws + l.ws_off[gi], bb.flags + l.flag_off[gi], g_ctx.stream));
+    if (g.tails) {
+      PersistPhase z{};
+      z.kind = kPhaseZero;
+      z.dep = -1;
+      z.n = uint64_t(1) << g.L;
+      z.batch = bb.desc + g.first;
+      z.count = g.nprod;
+      indep.push_back(z);
+    }
+  }
+  if (bp.nzero) {
+    PersistPhase z{};
+    z.kind = kPhaseZero;
+    z.dep = -1;
+    z.n = 0;
+    z.batch = bb.desc + bp.zero_first;
+    z.count = bp.nzero;
+    indep.push_back(z);
+  }
+  // Level by level across groups; each phase waits for its group's previous one.
+  std::vector<PersistPhase> out = indep;
+  std::vector<int> last(per.size(), -1);
+  size_t levels = 0;
+  for (const auto &v : per) levels = std::max(levels, v.size());
+  for (size_t lv = 0; lv < levels; ++lv)
+    for (size_t gi = 0; gi < per.size(); ++gi) {
+      if (lv >= per[gi].size()) continue;
+      PersistPhase p = per[gi][lv];
+      p.dep = lv == 0 ? -1 : last[gi];
+      last[gi] = static_cast<int>(out.size());
+      out.push_back(p);
+    }
+  if (out.size() > static_cast<size_t>(kPersistMaxPhases)) return HG_OK;
+  // Items of up to 8 units, but at least four items per CTA of the grid
+  // where the phase has that many units.
+  const uint64_t grid = static_cast<uint64_t>(persist_grid());
+  uint64_t first = 0;
+  for (PersistPhase &p : out) {
+    p.units = p.count;
+    p.per = std::max<uint64_t>(1, std::min<uint64_t>(8, p.units / (4 * grid)));
+    p.count = (p.units + p.per - 1) / p.per;
+    p.first = first;
+    first += p.count;
+  }
+  HG_CUDA(b->d_phases.ensure(out.size() * sizeof(PersistPhase)), "batch work list");
+  HG_CUDA(cudaMemcpy(b->d_phases.p, out.data(), out.size() * sizeof(PersistPhase), cudaMemcpyHostToDevice),
+          "batch work list upload");
+  HG_CUDA(b->d_state.ensure(persist_state_bytes(static_cast<int>(out.size()))), "batch work counters");
+  b->phases.swap(out);
+  b->items = first;
+  return HG_OK;
+}
+
+int persist_run(hg_batch *b, cudaStream_t st) {
+  const BatchBufs bb = batch_bufs(b);
+  if (b->persist_flag_words)
+    HG_CUDA(cudaMemsetAsync(bb.flags, 0, b->persist_flag_words * 8, st), "scan flags reset");
+  ProfScope ps(HG_KC_BATCH, st, 0.0);
+  HG_CUDA(launch_persist(static_cast<const PersistPhase *>(b->d_phases.p), static_cast<int>(b->phases.size()),
+                         b->items, static_cast<PersistState *>(b->d_state.p), bb.err, st),
+          "persistent batch");
+  return HG_OK;
+}
+
+int batch_clear_scan(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) {
+  if (bp.flag_words) HG_CUDA(cudaMemsetAsync(bb.flags, 0, bp.flag_words * 8, st), "scan flags reset");
+  if (!bp.groups.empty()) HG_CUDA(cudaMemsetAsync(bb.tickets, 0, bp.groups.size() * 8, st), "scan tickets reset");
+  return HG_OK;
 }
 
 // Time each candidate schedule of each group (twice; the second run counts)
@@ -1268,6 +1479,33 @@ int batch_autotune(hg_batch *b) {
   return rc;
 }
 
+// Time the whole batch on both schedules (twice each; the second run
+// counts) and keep the faster.
+int schedule_autotune(hg_batch *b) {
+  cudaStream_t st = g_ctx.stream;
+  cudaEvent_t e0, e1;
+  HG_CUDA(cudaEventCreate(&e0), "event creation");
+  HG_CUDA(cudaEventCreate(&e1), "event creation");
+  int rc = HG_OK;
+  float ms[2] = {0, 0};
+  for (int sched = 0; sched < 2 && rc == HG_OK; ++sched) {
+    b->persistent = sched == 1;
+    for (int rep = 0; rep < 2 && rc == HG_OK; ++rep) {
+      cudaEventRecord(e0, st);
+      rc = b->persistent ? persist_run(b, st) : enqueue_batch(b->bp, batch_bufs(b), st);
+      if (rc) break;
+      cudaEventRecord(e1, st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(HG_ERR_CUDA, "schedule timing failed");
+      else cudaEventElapsedTime(&ms[sched], e0, e1);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == HG_OK) rc = read_device_error(st);
+  b->persistent = ms[1] <= ms[0];
+  return rc;
+}
+
 constexpr uint64_t kBatchWorkspaceCap = uint64_t(4) << 30;  // bytes per group chunk
 
 // Validate the C-ABI product list into descriptors.
@@ -1308,6 +1546,8 @@ int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
   if (bp.ws_words) HG_CUDA(b->ws.ensure(bp.ws_words * 8), "batch workspace");
   if (bp.flag_words) HG_CUDA(b->flags.ensure(bp.flag_words * 8), "batch scan flags");
   HG_CUDA(b->tickets.ensure(std::max<size_t>(1, bp.groups.size()) * 8), "batch tickets");
+  if ((flags & HG_BATCH_PER_PASS) && (flags & HG_BATCH_PERSISTENT))
+    return fail(HG_ERR_ARG, "a batch runs either per pass or persistently, not both");
   if (flags & HG_BATCH_AUTOTUNE) {
     if ((rc = batch_autotune(b.get()))) return rc;
   } else {
@@ -1317,12 +1557,23 @@ int batch_create(const hg_product *prods, size_t n, int flags, hg_batch **out) {
       if (it != g_tuned.end()) g.plan = it->second;
     }
   }
+  if (!(flags & HG_BATCH_PER_PASS)) {
+    if ((rc = persist_build(b.get()))) return rc;
+    b->persistent = b->items > 0;
+    if ((flags & HG_BATCH_PERSISTENT) && !b->persistent && !b->bp.groups.empty())
+      return fail(HG_ERR_ARG, "this batch cannot run as one persistent launch (more than %d phases, or group "
+                              "workspaces above %llu bytes)", kPersistMaxPhases, (unsigned long long)kPersistWorkspaceCap);
+    if ((flags & HG_BATCH_AUTOTUNE) && !(flags & HG_BATCH_PERSISTENT) && b->persistent &&
+        (rc = schedule_autotune(b.get())))
+      return rc;
+  }
   *out = b.release();
   return HG_OK;
 }
 
 int batch_run(hg_batch *b, cudaStream_t st) {
   if (!b) return fail(HG_ERR_ARG, "null batch");
+  if (b->persistent) return persist_run(b, st);
   return enqueue_batch(b->bp, batch_bufs(b), st);
 }
 
@@ -1465,9 +1716,25 @@ int hg_batch_run(hg_batch *batch, void *stream) {
   return batch_run(batch, static_cast<cudaStream_t>(stream));
 }
 
+int hg_batch_schedule(const hg_batch *batch, int *persistent, size_t *launches) {
+  if (!batch || !persistent || !launches) return fail(HG_ERR_ARG, "null pointer");
+  *persistent = batch->persistent ? 1 : 0;
+  if (batch->persistent) {
+    *launches = 1;
+    return HG_OK;
+  }
+  size_t n = batch->bp.nzero ? 1 : 0;
+  for (const hg::BatchGroup &g : batch->bp.groups)
+    n += (g.tails ? 1 : 0) + 2 * (g.plan.size() - 1) + 1 + 2;  // zero tails, passes, middle, carry + fix
+  *launches = n;
+  return HG_OK;
+}
+
 int hg_batch_destroy(hg_batch *batch) {
   std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
   if (!batch) return HG_OK;
+  batch->d_phases.release();
+  batch->d_state.release();
   batch->d_desc.release();
   batch->ws.release();
   batch->flags.release();

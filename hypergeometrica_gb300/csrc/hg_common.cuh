@@ -37,6 +37,7 @@ enum DevErr : int {
   kDevCarryOverflow = 2,  // a carry left the top of the result
   kDevTicket = 3,         // a carry tile ticket fell outside its launch, or a tile aggregate of another launch
   kDevCopyTimeout = 4,    // a tile copy (TMA) did not land within its wait limit
+  kDevQueueTimeout = 5,   // a persistent batch's item waited past its limit for the phase before it
 };
 
 // Latch `code` in the device error word (the first error wins).

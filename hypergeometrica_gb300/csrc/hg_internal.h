@@ -155,4 +155,52 @@ cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse
 // Tiles a carry-scan launch over n positions uses.
 uint64_t carry_tiles(uint64_t n);
 
+// ---- one persistent launch for a batch (hg_persist.cu) --------------------
+//
+// A phase is one launch of the per-pass schedule; each of its items covers
+// `per` consecutive units (CTAs of that launch).  Items of a phase with
+// dep >= 0 start once phase dep has counted all its items done.
+enum PersistKind : int {
+  kPhaseZero = 0,     // out[n, nout) of products batch[0, count) (all of out when n == 0)
+  kPhaseStrided = 1,  // sel = logR | inverse << 4
+  kPhaseContig = 2,   // sel = T | mode << 4 (kContigMul or kContigSqr); item = by * gx + bx
+  kPhaseTiny = 3,     // sel = mode; 256 (product, prime) pairs per item
+  kPhaseCarry = 4,    // one carry tile of the persistent kernel per item
+  kPhaseFix = 5,      // eight carry tiles per item, one per warp
+};
+
+struct PersistPhase {
+  int kind, sel, dep, pad;
+  uint64_t first, count, gx;
+  uint64_t units, per;  // the launch's CTAs (warps for kPhaseFix, 256-pair groups for kPhaseTiny); per item
+  PassArgs a;
+  // reconstruction, carry and zeroing
+  const uint64_t *res;
+  uint64_t n, ws_stride, tpp, tiles;
+  CrtConst cc;
+  const ProductDesc *batch;
+  ScanState ss;
+};
+
+constexpr int kPersistMaxPhases = 512;
+constexpr size_t kPersistSmemBytes = 2 * (size_t(1) << kTileBits) * sizeof(uint64_t);
+
+// The work counter, the abort word and one completion count per phase.
+struct PersistState {
+  unsigned long long next;
+  unsigned abort, pad;
+  unsigned done[1];
+};
+__host__ __device__ constexpr size_t persist_state_bytes(int nphases) {
+  return sizeof(PersistState) + sizeof(unsigned) * static_cast<size_t>(nphases);
+}
+
+// CTAs of the persistent grid (SMs x resident CTAs per SM), 0 if unavailable.
+int persist_grid();
+// Carry tiles of the persistent kernel over n positions.
+uint64_t persist_carry_tiles(uint64_t n);
+// Clear the state and launch; phases and state are device memory.
+cudaError_t launch_persist(const PersistPhase *phases, int nphases, uint64_t total, PersistState *state, int *err,
+                           cudaStream_t st);
+
 }  // namespace hg

@@ -29,129 +29,23 @@
 #include <cudaTypedefs.h>
 #include <mutex>
 
-#include "hg_ntt_rounds.cuh"
+#include "hg_ntt_bodies.cuh"
 #include "hg_tma.cuh"
 
 namespace hg {
 namespace {
 
 using namespace rounds;
+using namespace bodies;
 
 // Four CTAs of 256 threads per SM (64 registers, a few spilled words): on
 // the 2^25-point passes faster than three (80 registers), two (128) or five
 // (48).
 template <int LOGR, bool INV>
 __global__ void __launch_bounds__(kTileThreads, 4) ntt_strided_kernel(const PassArgs P) {
-  constexpr int T = kTileBits;
-  constexpr int LOGTC = T - LOGR;  // log2 columns per tile
-  constexpr int ROWOFF = LOGTC;    // tile bit of row bit 0
-  constexpr int A0 = ROWOFF;       // register block of the low row group
-  constexpr int A1 = T - 4;        // register block of the top row group
-  constexpr int G = (LOGR + 3) / 4;
-  constexpr int NB1 = LOGR - 4;  // row bits of the top group (when G == 2)
-  static_assert(LOGR >= 4 && LOGR <= 8, "strided passes have 4..8 row bits");
   __shared__ ulonglong2 tw[1 << (LOGR - 1)];
-  __shared__ uint64_t sm[G == 2 ? (1 << T) : 1];
-
-  const uint32_t tid = threadIdx.x;
-  uint64_t bid = blockIdx.x;
-  const int prime = P.prime_lo + static_cast<int>(bid % P.nprimes);
-  bid /= P.nprimes;
-  const int op = static_cast<int>(bid % P.nops);
-  bid /= P.nops;
-  const uint64_t prod = bid / P.tiles;
-  const uint64_t tile = P.tile_lo + bid % P.tiles;
-
-  const uint64_t p = P.pc[prime].p;
-  const uint32_t c = P.pc[prime].c;
-  const NttTables tb = P.tb[prime];
-  uint64_t *data = P.data[op] + prod * P.ws_stride + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
-  const int logS = P.logS;
-  const int logM = LOGR + logS;
-  const uint64_t ncg = 1ull << (logS - LOGTC);
-  const uint64_t blk = tile / ncg, cg = tile % ncg;
-  const uint64_t base = (blk << logM) + (cg << LOGTC);
-  const uint64_t s0 = cg << LOGTC;
-
-  load_sub_twiddles(tw, INV ? tb.sub_inv : tb.sub_fwd, LOGR, tid, kTileThreads);
-
-  // Global offset of the thread's register 0 in layout A, and the stride
-  // between consecutive registers (register bits are row bits).
-  auto offsets = [&](uint32_t xt, int a, uint64_t &off0, uint64_t &step) {
-    off0 = base + (static_cast<uint64_t>(xt >> ROWOFF) << logS) + (xt & ((1u << LOGTC) - 1u));
-    step = 1ull << (logS + (a - ROWOFF));
-  };
-  // The inter-pass twiddles of the thread's 16 rows r = rhi * 16 + i of one
-  // column s (layout A0): from the pass table when there is one, else as the
-  // geometric sequence beta * gamma^bitrev4(i) from the two-level tables.
-  auto inter_pass = [&](uint64_t (&v)[16], uint32_t xt, const uint64_t *hi, const uint64_t *lo) {
-    const uint64_t s = s0 + (xt & ((1u << LOGTC) - 1u));
-    const uint32_t rhi = (xt >> (ROWOFF + 4)) & ((1u << (LOGR - 4)) - 1u);
-    if (P.ptw) {
-      const uint64_t *t = P.ptw + (static_cast<uint64_t>(prime) << logM) +
-                          (static_cast<uint64_t>(rhi) << (4 + logS)) + s;
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(t + (static_cast<uint64_t>(i) << logS)), p, c);
-      return;
-    }
-    uint32_t rrev = 0;
-    if constexpr (LOGR > 4) rrev = bitrev(rhi, LOGR - 4);
-    const uint64_t beta = table_twiddle(s * rrev, logM, hi, lo, p, c);
-    const uint64_t gamma = table_twiddle(s << (LOGR - 4), logM, hi, lo, p, c);
-    geometric_twiddle(v, beta, gamma, p, c);
-  };
-
-  uint64_t v[16];
-  if (!INV) {
-    constexpr int AL = (G == 2) ? A1 : A0;
-    uint32_t xt = thread_base<AL>(tid);
-    uint64_t off, step;
-    offsets(xt, AL, off, step);
-    uint64_t nl = 0;
-    const uint64_t *limbs = pass_limbs(P, prod, op, nl);
-    if (limbs) {
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const uint64_t o = off + i * step;
-        v[i] = o < nl ? reduce64(__ldg(limbs + o), p) : 0;
-      }
-    } else {
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
-    }
-    __syncthreads();  // twiddle table ready
-    if constexpr (G == 2) {
-      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false>(v, tw, xt, p, c);
-      to_smem<A1>(sm, v, xt);
-      __syncthreads();
-      xt = thread_base<A0>(tid);
-      from_smem<A0>(v, sm, xt);
-    }
-    stages<4, 0, A0, ROWOFF, 0, LOGR, false, true, true>(v, tw, xt, p, c);  // then the inter-pass twiddle
-    inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
-    offsets(xt, A0, off, step);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) data[off + i * step] = v[i];
-  } else {
-    uint32_t xt = thread_base<A0>(tid);
-    uint64_t off, step;
-    offsets(xt, A0, off, step);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
-    inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
-    __syncthreads();  // twiddle table ready
-    stages<4, 0, A0, ROWOFF, 0, LOGR, true, true, true>(v, tw, xt, p, c);  // after the inter-pass twiddle
-    if constexpr (G == 2) {
-      to_smem<A0>(sm, v, xt);
-      __syncthreads();
-      xt = thread_base<A1>(tid);
-      from_smem<A1>(v, sm, xt);
-      stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, true, false>(v, tw, xt, p, c);
-      offsets(xt, A1, off, step);
-    }
-#pragma unroll
-    for (int i = 0; i < 16; ++i) data[off + i * step] = v[i];
-  }
+  __shared__ uint64_t sm[LOGR > 4 ? (1 << kTileBits) : 1];
+  strided_ldg_body<LOGR, INV>(P, blockIdx.x, tw, sm);
 }
 
 // Tensor maps of one TMA-staged pass: the box each CTA loads (residues, or

@@ -85,20 +85,36 @@ class Batch:
     """A planned batch of products (hg_batch_create); run() enqueues it on a
     stream and can be captured in a CUDA graph.  Keeps the tensors alive."""
 
-    def __init__(self, items, autotune: bool = True):
+    def __init__(self, items, autotune: bool = True, schedule: str | None = None):
+        """schedule: None (the persistent launch, or with autotune the faster
+        of the two), "persistent" or "per_pass"."""
         import ctypes
 
-        from ._lib import HG_BATCH_AUTOTUNE
+        from ._lib import HG_BATCH_AUTOTUNE, HG_BATCH_PER_PASS, HG_BATCH_PERSISTENT
 
+        flags = HG_BATCH_AUTOTUNE if autotune else 0
+        if schedule == "persistent":
+            flags |= HG_BATCH_PERSISTENT
+        elif schedule == "per_pass":
+            flags |= HG_BATCH_PER_PASS
+        elif schedule is not None:
+            raise ValueError(f"unknown schedule {schedule!r}")
         self._items = list(items)
         self._arr = _products(self._items)
         h = ctypes.c_void_p()
-        check(load().hg_batch_create(self._arr, len(self._items), HG_BATCH_AUTOTUNE if autotune else 0,
-                                     ctypes.byref(h)))
+        check(load().hg_batch_create(self._arr, len(self._items), flags, ctypes.byref(h)))
         self._h = h
 
     def run(self, stream=None) -> None:
         check(load().hg_batch_run(self._h, _stream(stream)))
+
+    def schedule(self) -> tuple[str, int]:
+        """("persistent" or "per_pass", kernel launches per run)."""
+        import ctypes
+
+        pers, n = ctypes.c_int(), ctypes.c_size_t()
+        check(load().hg_batch_schedule(self._h, ctypes.byref(pers), ctypes.byref(n)))
+        return ("persistent" if pers.value else "per_pass"), n.value
 
     def close(self) -> None:
         if getattr(self, "_h", None):

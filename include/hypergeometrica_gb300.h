@@ -188,11 +188,15 @@ int hg_sync(void *stream);
  * No counterpart in the reference, which multiplies one pair at a time.  Its
  * binary splitting issues thousands of independent products per tree level
  * (combine, src/binary-splitting.lisp:112-121); a batch runs them together:
- * products are grouped by transform length and each group runs as one
- * launch per NTT pass, with the pass split per length chosen by timing the
- * candidates (HG_BATCH_AUTOTUNE).  hg_batch_run enqueues kernels and
- * memsets only, so it can be captured in a CUDA graph and replayed; a batch
- * owns its workspace, so batches on different streams may overlap. */
+ * products are grouped by transform length.  By default the whole batch
+ * runs as one persistent launch: a fixed grid of CTAs walks a device work
+ * list of (group, pass, tile) items, each group's passes in order and the
+ * groups overlapping.  The per-pass schedule instead runs each group as one
+ * launch per NTT pass.  HG_BATCH_AUTOTUNE times the candidate pass splits
+ * of each length, and then both schedules on the whole batch, and keeps the
+ * fastest.  hg_batch_run enqueues kernels and memsets only, so it can be
+ * captured in a CUDA graph and replayed; a batch owns its workspace, so
+ * batches on different streams may overlap. */
 typedef struct hg_product {
     const uint64_t *x; /* device limbs                                   */
     size_t nx;
@@ -203,7 +207,9 @@ typedef struct hg_product {
 } hg_product;
 
 typedef struct hg_batch hg_batch;
-#define HG_BATCH_AUTOTUNE 1 /* time the candidate pass splits for each length */
+#define HG_BATCH_AUTOTUNE 1   /* time the candidate pass splits and both schedules */
+#define HG_BATCH_PER_PASS 2   /* run one launch per pass per group (no persistent launch) */
+#define HG_BATCH_PERSISTENT 4 /* run as one persistent launch; HG_ERR_ARG if it cannot */
 
 /* Plan a batch (sizes as given: device operands are not trimmed), allocate
  * its workspace and, with HG_BATCH_AUTOTUNE, run each group once per
@@ -212,6 +218,9 @@ typedef struct hg_batch hg_batch;
 int hg_batch_create(const hg_product *prods, size_t n, int flags, hg_batch **batch);
 /* Enqueue every product of the batch on stream. */
 int hg_batch_run(hg_batch *batch, void *stream);
+/* The schedule a batch runs: *persistent = 1 for the one persistent launch,
+ * 0 for one launch per pass; *launches = kernel launches per hg_batch_run. */
+int hg_batch_schedule(const hg_batch *batch, int *persistent, size_t *launches);
 /* Free a batch (after its work has completed). */
 int hg_batch_destroy(hg_batch *batch);
 /* One-shot: create (no tuning, schedules from earlier tuning are reused),
@@ -362,7 +371,8 @@ int hg_ntt_reverse_device(uint64_t *a, size_t n, int mod_num, void *stream);
 #define HG_KC_CARRY 3       /* reconstruction + carry scan                      */
 #define HG_KC_SMALL 4       /* schoolboy / by-digit products                    */
 #define HG_KC_OTHER 5       /* scaling and other helpers                        */
-#define HG_KC_COUNT 6
+#define HG_KC_BATCH 6       /* a whole batch in one persistent launch           */
+#define HG_KC_COUNT 7
 
 /* Record a CUDA event pair around every kernel launch from now on (on != 0)
  * or stop recording (on == 0). */

@@ -195,3 +195,70 @@ def test_graph_capture_before_any_warm_run(hg):
     D.mul(x, y, want)
     D.sync()
     assert torch.equal(got[0], want) and torch.equal(got[1], want)
+
+
+@pytest.mark.parametrize("seed,count,lo,hi", [(21, 500, 0, 14), (22, 40, 10, 16), (23, 6, 14, 17), (24, 2, 20, 20)])
+def test_persistent_launch_matches_per_pass(hg, seed, count, lo, hi):
+    """The whole batch as one persistent launch (a work list of group, pass
+    and tile items) gives the same limbs as the per-pass schedule and as the
+    products computed alone: transform lengths from 2^1 (the in-register
+    transforms) to 2^21, squares, result
+    tails past the product, and an empty operand; 2^21-point products run
+    two strided passes each way."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+
+    items, host = _make(count, seed, lo_bits=lo, hi_bits=hi, extra_out=9)
+    zx = torch.zeros(1, dtype=torch.int64, device="cuda")
+    items.append((zx, _dev(W.limbs(3, 5)), torch.full((8,), -1, dtype=torch.int64, device="cuda"), 0, 5))
+    host.append((np.zeros(0, dtype=np.uint64), W.limbs(3, 5)))
+    outs = {}
+    for sched in ("per_pass", "persistent"):
+        for it in items:
+            it[2].fill_(-1)
+        b = D.Batch(items, autotune=False, schedule=sched)
+        kind, launches = b.schedule()
+        assert kind == sched
+        if sched == "persistent":
+            assert launches == 1
+        for _ in range(2):  # a second run reuses the work list and the counters
+            b.run()
+            D.sync()
+        outs[sched] = [_host(it[2]).copy() for it in items]
+        b.close()
+    for k in range(len(items)):
+        assert np.array_equal(outs["persistent"][k], outs["per_pass"][k]), k
+    for k in range(0, len(items), max(1, len(items) // 40)):
+        x, y = host[k]
+        if len(x) == 0:
+            assert not outs["persistent"][k].any()
+            continue
+        assert np.array_equal(outs["persistent"][k], _single(hg, x, y, len(outs["persistent"][k]))), k
+
+
+def test_persistent_launch_in_a_graph(hg):
+    """The persistent launch captured in a CUDA graph replays bit-identically."""
+    import torch
+
+    from hypergeometrica_gb300 import device as D
+
+    items, _ = _make(200, 31, lo_bits=4, hi_bits=14)
+    b = D.Batch(items, autotune=False, schedule="persistent")
+    b.run()
+    D.sync()
+    want = [_host(it[2]).copy() for it in items]
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        b.run(s)
+    for _ in range(3):
+        for it in items:
+            it[2].fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        D.sync()
+        for k, it in enumerate(items):
+            assert np.array_equal(_host(it[2]), want[k]), k
+    b.close()
