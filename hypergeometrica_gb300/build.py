@@ -42,7 +42,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(ROOT, "include", "hypergeometrica_gb300.h"))
     cc = nvcc()
     jobs = []

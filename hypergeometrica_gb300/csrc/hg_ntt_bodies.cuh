@@ -243,100 +243,7 @@ __host__ __device__ constexpr int contig_min_blocks(int T) { return (T >= 9 && T
 // launch; smem holds (MODE == kMul ? 2 : 1) * 4096 words.
 template <int T, int MODE>
 __device__ __forceinline__ void contig_body(const PassArgs &P, uint64_t bx, int by, uint64_t *smem) {
-  using Gr = Groups<T>;
-  constexpr int ATOP = Gr::template A<Gr::G - 1>();
-  constexpr int A0 = Gr::template A<0>();
-  constexpr int LT = T - 4;                  // log2 threads per block
-  constexpr int NT = kTileThreads;
-  constexpr int BPC = 1 << (kTileBits - T);  // blocks per CTA: every CTA has 256 threads
-  const uint32_t tid = threadIdx.x;
-  const uint32_t lt = tid & ((1u << LT) - 1u);  // thread within its block
-  const uint32_t lb = tid >> LT;                // block within the CTA
-  const int prime = P.prime_lo + by;
-  const uint64_t nblk = P.nprod * P.tiles;      // blocks of this prime
-  const uint64_t gb = bx * BPC + lb;
-  const bool valid = gb < nblk;                 // idle block slots still take part in barriers
-  const uint64_t prod = valid ? gb / P.tiles : 0;
-  const uint64_t tile = valid ? gb % P.tiles : 0;
-  const uint64_t p = P.pc[prime].p;
-  const uint32_t c = P.pc[prime].c;
-  const NttTables tb = P.tb[prime];
-  const uint64_t poff = prod * P.ws_stride + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride;
-  const uint64_t base = tile << T;
-
-  constexpr bool TWO = (MODE == kMul);
-  uint64_t *smA = smem + (lb << T);
-  uint64_t *smB = smem + ((BPC + lb) << T);
-  // The (twiddle, companion) pairs of the 2^T-point sub-transform, read from
-  // the swizzled device tables (small, and shared by every CTA: they stay in
-  // L1), forward first, inverse after the pointwise product.
-  const ulonglong2 *tw = swz_table(tb, T, MODE == kInv);
-  uint64_t nl0 = 0, nl1 = 0;
-  const uint64_t *limbs0 = pass_limbs(P, prod, 0, nl0);
-  const uint64_t *limbs1 = TWO ? pass_limbs(P, prod, 1, nl1) : nullptr;
-
-  uint64_t v[16];
-  uint32_t xt;
-  if constexpr (MODE == kInv) {
-    xt = thread_base<A0>(lt);
-    if (valid) load_block<A0>(v, P.data[0] + poff, nullptr, 0, base, xt, p);
-    else zero16(v);
-    inverse_rounds<T>(v, smA, tw, xt, lt, p, c);
-    if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
-    return;
-  } else if constexpr (MODE == kFwd) {
-    xt = thread_base<ATOP>(lt);
-    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
-    else zero16(v);
-    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
-    if (valid) store_block<A0>(v, P.data[0] + poff, base, xt);
-    return;
-  } else if constexpr (MODE == kMulSpec) {
-    xt = thread_base<ATOP>(lt);
-    if (valid) load_block<ATOP>(v, P.data[0] + poff, limbs0, nl0, base, xt, p);
-    else zero16(v);
-    forward_rounds<T>(v, smA, tw, xt, lt, p, c);
-    // The shared spectrum sits where kFwd stores it, without a product offset.
-    if (valid) {
-      const uint64_t *spec = P.data[1] + static_cast<uint64_t>(prime - P.prime_lo) * P.prime_stride + base;
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], __ldg(spec + (xt | (static_cast<uint32_t>(i) << A0))), p, c);
-    }
-    inverse_rounds<T, true>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
-    if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
-    return;
-  } else {
-    {
-      // The operands' forward transforms share one copy of the round code (a
-      // loop, not unrolled): operand 0's spectrum is parked in smA (each
-      // thread rereads only its own words), operand 1 transforms through smB.
-      constexpr int nop = TWO ? 2 : 1;
-#pragma unroll 1
-      for (int op = 0; op < nop; ++op) {
-        xt = thread_base<ATOP>(lt);
-        if (valid) load_block<ATOP>(v, P.data[op] + poff, op ? limbs1 : limbs0, op ? nl1 : nl0, base, xt, p);
-        else zero16(v);
-        forward_rounds<T>(v, op ? smB : smA, tw, xt, lt, p, c);
-        if (TWO && op == 0) {
-          __syncthreads();
-          to_smem<A0>(smA, v, xt);
-        }
-      }
-    }
-    {
-      if constexpr (MODE == kMul) {
-        const uint32_t sx = swz(xt);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = mont_mul(smA[sx ^ swz(static_cast<uint32_t>(i) << A0)], v[i], p, c);
-      } else {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = mont_mul(v[i], v[i], p, c);
-      }
-      // The product is x*y*2^-64; the reconstruction constants absorb 2^64.
-      inverse_rounds<T, true>(v, smA, swz_table(tb, T, true), xt, lt, p, c);
-      if (valid) store_block<ATOP>(v, P.data[0] + poff, base, xt);
-    }
-  }
+#include "hg_contig_body.inc"
 }
 
 // Transforms of 2, 4 or 8 points: the reference's loops, one thread per

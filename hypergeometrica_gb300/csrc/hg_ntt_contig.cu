@@ -31,7 +31,9 @@ using namespace bodies;
 template <int T, int MODE>
 __global__ void __launch_bounds__(kTileThreads, contig_min_blocks(T)) ntt_contig_kernel(const PassArgs P) {
   extern __shared__ uint64_t smem[];
-  contig_body<T, MODE>(P, blockIdx.x, static_cast<int>(blockIdx.y), smem);
+  const uint64_t bx = blockIdx.x;
+  const int by = static_cast<int>(blockIdx.y);
+#include "hg_contig_body.inc"
 }
 
 __global__ void ntt_tiny_kernel(const PassArgs P, int mode) {
