@@ -14,6 +14,9 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "libhg_gb300.so")
+# HG_CHECKED=1 in the environment loads the checked build instead (range,
+# bounds and product checks in every kernel; see hg_build_checked).
+CHECKED_LIB_PATH = os.path.join(HERE, "libhg_gb300_checked.so")
 HEADER = os.path.join(ROOT, "include", "hypergeometrica_gb300.h")
 
 HG_OK = 0
@@ -83,6 +86,7 @@ SIGNATURES = {
     "hg_init_scheme": (ctypes.c_int, [_u64p, ctypes.c_int, _u64p, ctypes.c_int, ctypes.c_int]),
     "hg_shutdown": (ctypes.c_int, []),
     "hg_last_error": (ctypes.c_int, [ctypes.c_char_p, _sz]),
+    "hg_build_checked": (ctypes.c_int, []),
     "hg_scheme_moduli": (ctypes.c_int, [_u64p, ctypes.c_int]),
     "hg_ntt_length": (_sz, [_sz, _sz]),
     "hg_chunk_plan": (ctypes.c_int, [_sz, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
@@ -176,9 +180,11 @@ def load() -> ctypes.CDLL:
     with _lock:
         if _lib is not None:
             return _lib
-        if not os.path.exists(LIB_PATH):
-            raise HGError(HG_ERR_NOT_INIT, f"{LIB_PATH} is not built; run `python -m hypergeometrica_gb300.build`")
-        lib = ctypes.CDLL(LIB_PATH)
+        path = CHECKED_LIB_PATH if os.environ.get("HG_CHECKED") == "1" else LIB_PATH
+        if not os.path.exists(path):
+            raise HGError(HG_ERR_NOT_INIT, f"{path} is not built; run `python -m hypergeometrica_gb300.build`"
+                          + (" --checked" if path == CHECKED_LIB_PATH else ""))
+        lib = ctypes.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.restype = res

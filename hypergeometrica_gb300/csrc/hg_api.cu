@@ -982,11 +982,37 @@ int small_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   return HG_OK;
 }
 
+#if HG_CHECKED
+// The first fault a check latched in any translation unit since the last read.
+int read_checked_faults() {
+  static int (*const readers[])() = {checked_fault_strided, checked_fault_contig, checked_fault_crt,
+                                     checked_fault_persist, checked_fault_peak,   checked_fault_sum,
+                                     checked_fault_series};
+  int first = 0;
+  for (auto r : readers) {
+    const int v = r();
+    if (v && !first) first = v;
+  }
+  if (first == kDevRange) return fail(HG_ERR_INCONSISTENT, "checked build: a residue left its range");
+  if (first == kDevBounds) return fail(HG_ERR_INCONSISTENT, "checked build: a residue index left its array");
+  if (first == kDevProduct)
+    return fail(HG_ERR_INCONSISTENT, "checked build: a modular product differs from the exact reduction");
+  if (first) return fail(HG_ERR_CUDA, "checked build: fault word unreadable or code %d", first);
+  return HG_OK;
+}
+#endif
+
 int read_device_error(cudaStream_t st) {
   int err = 0;
   int *d_err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
   HG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st), "error word read");
   HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
+#if HG_CHECKED
+  {
+    const int rc = read_checked_faults();
+    if (rc) return rc;
+  }
+#endif
   if (err) {
     HG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st), "error word reset");
     HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
@@ -1802,6 +1828,8 @@ int hg_shutdown(void) {
   for (uint64_t *&p : g_noalloc_ptr) p = nullptr;
   return HG_OK;
 }
+
+int hg_build_checked(void) { return HG_CHECKED ? 1 : 0; }
 
 int hg_last_error(char *buf, size_t len) {
   if (!buf || len == 0) return HG_ERR_ARG;

@@ -88,6 +88,9 @@ struct CrtProducerT {
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
+    check_below(r0, 2 * p0);  // inverse residues live in [0, 2p)
+    check_below(r1, 2 * p1);
+    check_below(r2, 2 * p2);
     const uint64_t y0 = shoup_mul(r0, k.k0.x, k.k0.y, p0, c0);
     const uint64_t t1 =
         sub_mod_borrow(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);

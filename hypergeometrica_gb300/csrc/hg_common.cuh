@@ -38,7 +38,93 @@ enum DevErr : int {
   kDevTicket = 3,         // a carry tile ticket fell outside its launch, or a tile aggregate of another launch
   kDevCopyTimeout = 4,    // a tile copy (TMA) did not land within its wait limit
   kDevQueueTimeout = 5,   // a persistent batch's item waited past its limit for the phase before it
+  // Checked builds (HG_CHECKED) only:
+  kDevRange = 6,          // a residue outside the range its pass guarantees (>= p, or >= 2p)
+  kDevBounds = 7,         // a residue index outside its array; the access was skipped
+  kDevProduct = 8,        // a modular product that differs from an exact 128-bit reduction
 };
+
+// ---- checked builds -------------------------------------------------------
+//
+// Built with -DHG_CHECKED=1 (libhg_gb300_checked.so), the kernels check what
+// the reference checks under :hypergeometrica-safe and -paranoid
+// (src/config.lisp:31-37): every residue a pass reads or writes lies in its
+// range (ntt-forward asserts its inputs are below m,
+// src/number-theoretic-transform.lisp:63-64), every residue index lies in
+// its array, and every modular product equals an independent reduction of
+// the full 128-bit product (m*/fast2 re-checks against bignum mod,
+// src/modular-arithmetic.lisp:228-229).  A failed check latches a code in a
+// fault word of the translation unit (one per .cu file, read and cleared by
+// the host at hg_sync); an index out of range also skips the access.
+#ifndef HG_CHECKED
+#define HG_CHECKED 0
+#endif
+
+#if HG_CHECKED
+static __device__ int g_checked_fault;
+// Host: the fault word of this translation unit, cleared once read.
+#define HG_CHECKED_READER(name)                                                     \
+  int name() {                                                                      \
+    int v = 0;                                                                      \
+    if (cudaMemcpyFromSymbol(&v, g_checked_fault, sizeof v) != cudaSuccess) {       \
+      cudaGetLastError();                                                           \
+      return -1;                                                                    \
+    }                                                                               \
+    if (v) {                                                                        \
+      const int z = 0;                                                              \
+      cudaMemcpyToSymbol(g_checked_fault, &z, sizeof z);                            \
+    }                                                                               \
+    return v;                                                                       \
+  }
+#endif
+
+__device__ __forceinline__ void checked_fault(int code) {
+#if HG_CHECKED
+  atomicCAS(&g_checked_fault, 0, code);
+#else
+  (void)code;
+#endif
+}
+
+// x < bound, checked (checked builds only; nothing otherwise).
+__device__ __forceinline__ void check_below(uint64_t x, uint64_t bound) {
+#if HG_CHECKED
+  if (x >= bound) checked_fault(kDevRange);
+#else
+  (void)x;
+  (void)bound;
+#endif
+}
+
+// Index o < n, checked: false (and a fault latched) when it is not.  Always
+// true in unchecked builds.
+__device__ __forceinline__ bool check_index(uint64_t o, uint64_t n) {
+#if HG_CHECKED
+  if (o >= n) {
+    checked_fault(kDevBounds);
+    return false;
+  }
+#else
+  (void)o;
+  (void)n;
+#endif
+  return true;
+}
+
+#if HG_CHECKED
+// (a * b) mod p by binary long division of the 128-bit product, one bit at a
+// time: the independent reduction checked builds compare every product with.
+static __device__ __noinline__ uint64_t mulmod_exact(uint64_t a, uint64_t b, uint64_t p) {
+  const uint64_t lo = a * b, hi = __umul64hi(a, b);
+  uint64_t r = 0;  // r < p < 2^63, so 2r + 1 fits
+  for (int i = 127; i >= 0; --i) {
+    const uint64_t bit = i >= 64 ? (hi >> (i - 64)) & 1u : (lo >> i) & 1u;
+    r = (r << 1) | bit;
+    if (r >= p) r -= p;
+  }
+  return r;
+}
+#endif
 
 // Latch `code` in the device error word (the first error wins).
 __device__ __forceinline__ void latch_error(int *err, int code) {
@@ -133,7 +219,13 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
       : "=l"(mph)
       : "r"(static_cast<uint32_t>(t)), "r"(static_cast<uint32_t>(u)));
   mph += static_cast<uint64_t>(static_cast<uint32_t>(u >> 32)) << 55;
-  return hi >= mph ? hi - mph : hi - mph + p;  // low halves cancel exactly; hi, mph < p
+  const uint64_t r = hi >= mph ? hi - mph : hi - mph + p;  // low halves cancel exactly; hi, mph < p
+#if HG_CHECKED
+  // r 2^64 = a b (mod p), with 2^64 mod p = (2^32)^2 mod p
+  if (r >= p || mulmod_exact(r, mulmod_exact(1ull << 32, 1ull << 32, p), p) != mulmod_exact(a, b, p))
+    checked_fault(kDevProduct);
+#endif
+  return r;
 }
 
 // Shoup product a * w mod p for any 64-bit a, w < p with companion
@@ -143,7 +235,11 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
 __device__ __forceinline__ uint64_t shoup_mul(uint64_t a, uint64_t w, uint64_t wq, uint64_t p, uint32_t c) {
   const uint64_t q = mul_hi64(a, wq);
   const uint64_t r = a * w - q - (static_cast<uint64_t>(static_cast<uint32_t>(q) * (c << 23)) << 32);
-  return fold_p(r, p);
+  const uint64_t out = fold_p(r, p);
+#if HG_CHECKED
+  if (out != mulmod_exact(a, w, p)) checked_fault(kDevProduct);
+#endif
+  return out;
 }
 
 // x mod p for any 64-bit x (x < 4p because p > 2^62).

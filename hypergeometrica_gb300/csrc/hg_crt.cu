@@ -346,4 +346,8 @@ cudaError_t launch_digit_carry(const uint64_t *x, uint64_t nx, uint64_t d, uint6
   return launch_carry(ConvProducer{x, nx, nullptr, 1, d}, out, nproc, tiles, ss, st);
 }
 
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_crt)
+#endif
+
 }  // namespace hg

@@ -155,6 +155,18 @@ cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse
 // Tiles a carry-scan launch over n positions uses.
 uint64_t carry_tiles(uint64_t n);
 
+#if HG_CHECKED
+// The fault word of each translation unit with kernels (checked builds),
+// read and cleared: 0, a DevErr code, or -1 when the read failed.
+int checked_fault_strided();
+int checked_fault_contig();
+int checked_fault_crt();
+int checked_fault_persist();
+int checked_fault_peak();
+int checked_fault_sum();
+int checked_fault_series();
+#endif
+
 // ---- one persistent launch for a batch (hg_persist.cu) --------------------
 //
 // A phase is one launch of the per-pass schedule; each of its items covers

@@ -96,7 +96,11 @@ __device__ __forceinline__ void strided_ldg_body(const PassArgs &P, uint64_t bid
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
+      for (int i = 0; i < 16; ++i) {
+        const uint64_t o = off + i * step;
+        v[i] = check_index(o, uint64_t(1) << P.logN) ? data[o] : 0;
+        check_below(v[i], p);
+      }
     }
     __syncthreads();  // twiddle table ready
     if constexpr (G == 2) {
@@ -110,13 +114,21 @@ __device__ __forceinline__ void strided_ldg_body(const PassArgs &P, uint64_t bid
     inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
     offsets(xt, A0, off, step);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) data[off + i * step] = v[i];
+    for (int i = 0; i < 16; ++i) {
+      const uint64_t o = off + i * step;
+      check_below(v[i], p);
+      if (check_index(o, uint64_t(1) << P.logN)) data[o] = v[i];
+    }
   } else {
     uint32_t xt = thread_base<A0>(tid);
     uint64_t off, step;
     offsets(xt, A0, off, step);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = data[off + i * step];
+    for (int i = 0; i < 16; ++i) {
+      const uint64_t o = off + i * step;
+      v[i] = check_index(o, uint64_t(1) << P.logN) ? data[o] : 0;
+      check_below(v[i], 2 * p);
+    }
     inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
     __syncthreads();  // twiddle table ready
     stages<4, 0, A0, ROWOFF, 0, LOGR, true, true, true>(v, tw, xt, p, c);  // after the inter-pass twiddle
@@ -129,7 +141,11 @@ __device__ __forceinline__ void strided_ldg_body(const PassArgs &P, uint64_t bid
       offsets(xt, A1, off, step);
     }
 #pragma unroll
-    for (int i = 0; i < 16; ++i) data[off + i * step] = v[i];
+    for (int i = 0; i < 16; ++i) {
+      const uint64_t o = off + i * step;
+      check_below(v[i], 2 * p);
+      if (check_index(o, uint64_t(1) << P.logN)) data[o] = v[i];
+    }
   }
 }
 
@@ -209,9 +225,11 @@ __device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, 
   }
 }
 
+// Residues read here lie below `bound` (p for a forward input, 2p for an
+// inverse one), checked in checked builds.
 template <int A>
 __device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *data, const uint64_t *limbs, uint64_t nl,
-                                           uint64_t base, uint32_t xt, uint64_t p) {
+                                           uint64_t base, uint32_t xt, uint64_t p, uint64_t bound = 0) {
   if (limbs) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -220,7 +238,10 @@ __device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *da
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = data[base + (xt | (static_cast<uint32_t>(i) << A))];
+    for (int i = 0; i < 16; ++i) {
+      v[i] = data[base + (xt | (static_cast<uint32_t>(i) << A))];
+      check_below(v[i], bound ? bound : p);
+    }
   }
 }
 
@@ -230,9 +251,13 @@ __device__ __forceinline__ void zero16(uint64_t (&v)[16]) {
 }
 
 template <int A>
-__device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *data, uint64_t base, uint32_t xt) {
+__device__ __forceinline__ void store_block(const uint64_t (&v)[16], uint64_t *data, uint64_t base, uint32_t xt,
+                                            uint64_t bound = ~0ull) {
 #pragma unroll
-  for (int i = 0; i < 16; ++i) data[base + (xt | (static_cast<uint32_t>(i) << A))] = v[i];
+  for (int i = 0; i < 16; ++i) {
+    check_below(v[i], bound);
+    data[base + (xt | (static_cast<uint32_t>(i) << A))] = v[i];
+  }
 }
 
 // CTAs of 256 threads per SM: three (80 registers) where the rounds fit

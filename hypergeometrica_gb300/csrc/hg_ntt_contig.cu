@@ -84,6 +84,10 @@ cudaError_t launch_mode(const PassArgs &a, uint64_t nblk, cudaStream_t st) {
 
 }  // namespace
 
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_contig)
+#endif
+
 cudaError_t launch_ntt_contig(const PassArgs &a, int mode, cudaStream_t st) {
   const uint64_t nblk = a.tiles * a.nprod;  // blocks per prime
   if (nblk == 0 || a.logS != 0 || a.logR != a.logT || a.nprimes < 1 || a.nprimes > kPrimes)

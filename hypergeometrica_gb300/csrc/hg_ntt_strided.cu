@@ -173,7 +173,10 @@ __global__ void __launch_bounds__(kTileThreads, 3)
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = tile[xt | (static_cast<uint32_t>(i) << AL)];
+      for (int i = 0; i < 16; ++i) {
+        v[i] = tile[xt | (static_cast<uint32_t>(i) << AL)];
+        check_below(v[i], p);  // forward input: canonical residues
+      }
     }
     if constexpr (G == 2) {
       if (LIMBS && ((L.ztop >> op) & 1))
@@ -190,11 +193,17 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     inter_pass(v, xt, tb.hi_fwd, tb.lo_fwd);
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 16; ++i) tile[xt | (static_cast<uint32_t>(i) << A0)] = v[i];
+    for (int i = 0; i < 16; ++i) {
+      check_below(v[i], p);  // after the Montgomery inter-pass twiddle
+      tile[xt | (static_cast<uint32_t>(i) << A0)] = v[i];
+    }
   } else {
     xt = thread_base<A0>(tid);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = tile[xt | (static_cast<uint32_t>(i) << A0)];
+    for (int i = 0; i < 16; ++i) {
+      v[i] = tile[xt | (static_cast<uint32_t>(i) << A0)];
+      check_below(v[i], 2 * p);  // inverse residues live in [0, 2p)
+    }
     inter_pass(v, xt, tb.hi_inv, tb.lo_inv);
     stages<4, 0, A0, ROWOFF, 0, LOGR, true, true, true>(v, tw, xt, p, c);
     constexpr int AS = (G == 2) ? A1 : A0;
@@ -208,7 +217,10 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 16; ++i) tile[xt | (static_cast<uint32_t>(i) << AS)] = v[i];
+    for (int i = 0; i < 16; ++i) {
+      check_below(v[i], 2 * p);
+      tile[xt | (static_cast<uint32_t>(i) << AS)] = v[i];
+    }
   }
   tma::fence_async_smem();
   __syncthreads();
@@ -364,6 +376,10 @@ bool tma_aligned(const PassArgs &a) {
 }
 
 }  // namespace
+
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_strided)
+#endif
 
 cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse, const NttTables *tb,
                                  const PrimeConst *pc, int nprimes, cudaStream_t st) {

@@ -93,4 +93,8 @@ int butterfly_peak(double *per_s, const PrimeConst &pc, const ulonglong2 *table)
   return HG_OK;
 }
 
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_peak)
+#endif
+
 }  // namespace hg

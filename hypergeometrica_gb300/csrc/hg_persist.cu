@@ -254,4 +254,8 @@ cudaError_t launch_persist(const PersistPhase *phases, int nphases, uint64_t tot
   return cudaGetLastError();
 }
 
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_persist)
+#endif
+
 }  // namespace hg

@@ -285,6 +285,10 @@ __global__ void nodes_kernel(hg_poly pa, hg_poly pb, hg_poly pp, hg_poly pq, con
 }
 
 }  // namespace
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_series)
+#endif
+
 }  // namespace hg
 
 using namespace hg;

@@ -261,6 +261,10 @@ int run_batch(const Desc *host, size_t n, cudaStream_t st, const char *what, Lau
 }
 
 }  // namespace
+#if HG_CHECKED
+HG_CHECKED_READER(checked_fault_sum)
+#endif
+
 }  // namespace hg
 
 using namespace hg;

@@ -74,6 +74,18 @@ int hg_shutdown(void);
 /* Copy the message of the last error on this thread into buf. */
 int hg_last_error(char *buf, size_t len);
 
+/* 1 when this library is the checked build (libhg_gb300_checked.so), which
+ * does what the reference does under :hypergeometrica-safe and -paranoid
+ * (src/config.lisp:31-37): every residue a pass reads or writes is checked
+ * against its range (ntt-forward's input assertion,
+ * src/number-theoretic-transform.lisp:63-64), every residue index against
+ * its array, and every modular product against an exact reduction of the
+ * 128-bit product (the paranoid re-check of the reference's Shoup product,
+ * src/modular-arithmetic.lisp:228-229).
+ * A failed check is reported by the next hg_sync (or host-memory call) as
+ * HG_ERR_INCONSISTENT.  0 for the regular build. */
+int hg_build_checked(void);
+
 /* Number of moduli and their values, largest first (scheme-moduli). */
 int hg_scheme_moduli(uint64_t *out, int cap);
 

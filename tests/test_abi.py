@@ -34,6 +34,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_host_only_queries(lib):
+    assert lib.hg_build_checked() == 0  # the regular build; HG_CHECKED=1 selects the checked one
     assert lib.hg_ntt_length(3, 5) == 8
     assert lib.hg_ntt_length(4096, 4096) == 8192
     assert lib.hg_ntt_length(4097, 4096) == 16384
