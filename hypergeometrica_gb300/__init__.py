@@ -19,6 +19,7 @@ from .mpz import (  # noqa: F401
     mpz_multiply_by_digit,
     mpz_size,
     mpz_square,
+    mul_host_pipeline,
     multiply_storage_schoolboy,
     scheme_moduli,
 )
@@ -38,6 +39,7 @@ __all__ = [
     "mpz_multiply_by_digit",
     "mpz_size",
     "mpz_square",
+    "mul_host_pipeline",
     "multiply_storage_schoolboy",
     "scheme_moduli",
 ]

@@ -52,6 +52,12 @@ _sz = ctypes.c_size_t
 _vp = ctypes.c_void_p
 
 
+class HgHostProduct(ctypes.Structure):
+    """hg_host_product: one product of hg_mul_host_pipeline (host pointers; y NULL squares x)."""
+
+    _fields_ = [("x", _vp), ("nx", _sz), ("y", _vp), ("ny", _sz), ("out", _vp), ("nout", _sz)]
+
+
 class HgProduct(ctypes.Structure):
     """hg_product: one product of a batch (device pointers; y NULL squares x)."""
 
@@ -93,6 +99,7 @@ SIGNATURES = {
     "hg_set_chunking": (ctypes.c_int, [ctypes.c_int]),
     "hg_mul": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
     "hg_sqr": (ctypes.c_int, [_vp, _sz, _vp, _sz]),
+    "hg_mul_host_pipeline": (ctypes.c_int, [ctypes.POINTER(HgHostProduct), _sz]),
     "hg_mul_schoolboy": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _sz]),
     "hg_mul_digit": (ctypes.c_int, [_vp, _sz, ctypes.c_uint64, _vp, _sz]),
     "hg_mpz_mul": (ctypes.c_int, [_vp, _sz, ctypes.c_int, _vp, _sz, ctypes.c_int, ctypes.c_int, _sz, _vp, _sz,

@@ -122,6 +122,27 @@ struct DevBuf {
 // Column slices of an operand upload from host memory (ntt_product_device).
 constexpr int kUploadSlices = 4;
 
+// The streams, workspace and carry-scan state one product at a time runs
+// in.  Every entry point uses lane 0; hg_mul_host_pipeline alternates
+// between the lanes so that one product's download and the next one's
+// upload and transforms overlap.
+struct Lane {
+  cudaStream_t stream = nullptr;
+  DevBuf A, B, X, Y, OUT, flags;
+  DevBuf misc;  // bytes [0, 8) carry-scan ticket, [8, 12) error word (lane 0's is the library's), [16, 24) large-sum top index
+  unsigned long long ticket_count = 0;
+  uint32_t epoch = 0;
+  cudaEvent_t ws_done = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host entry points: operand uploads
+  cudaEvent_t copy_done = nullptr;
+  cudaEvent_t slice_done[2][kUploadSlices] = {};  // per operand, per column slice of the upload
+  bool ws_pending = false;
+  cudaStream_t d2h_stream = nullptr;  // hg_mul_host_pipeline: product downloads
+  cudaEvent_t carry_done = nullptr, d2h_done = nullptr;
+  bool d2h_pending = false;
+};
+constexpr int kLanes = 2;
+
 struct Context {
   bool ready = false;
   int device = 0;
@@ -130,20 +151,15 @@ struct Context {
   PrimeConst pc[kPrimes] = {};
   NttTables tb[kPrimes] = {};
   DevBuf tables;
-  cudaStream_t stream = nullptr;
-  DevBuf A, B, X, Y, OUT, flags;
-  DevBuf misc;  // bytes [0, 8) carry-scan ticket, [8, 12) error word, [16, 24) large-sum top index
-  unsigned long long ticket_count = 0;
-  uint32_t epoch = 0;
-  cudaEvent_t ws_done = nullptr;
-  cudaStream_t copy_stream = nullptr;  // host entry points: operand uploads
-  cudaEvent_t copy_done = nullptr;
-  cudaEvent_t slice_done[2][kUploadSlices] = {};  // per operand, per column slice of the upload
-  bool ws_pending = false;
+  Lane lanes[kLanes];
+  Lane *lane = &lanes[0];  // the lane products are enqueued in
   std::recursive_mutex mu;
 };
 
 Context g_ctx;
+
+// The library's device error word (lane 0's); every lane's kernels latch here.
+int *err_word() { return reinterpret_cast<int *>(static_cast<char *>(g_ctx.lanes[0].misc.p) + 8); }
 thread_local std::string t_err;
 
 // ---- instrumentation: launch counters and optional event timing ---------
@@ -342,14 +358,20 @@ int init_locked(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg,
     c.tb[i].lo_inv = c.tb[i].hi_inv + kLevelWords;
     c.tb[i].swz = reinterpret_cast<const ulonglong2 *>(t + 2 * kSubWords + 4 * kLevelWords);
   }
-  HG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream creation");
-  HG_CUDA(cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming), "event creation");
-  HG_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking), "stream creation");
-  HG_CUDA(cudaEventCreateWithFlags(&c.copy_done, cudaEventDisableTiming), "event creation");
-  for (auto &op : c.slice_done)
-    for (cudaEvent_t &e : op) HG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event creation");
-  HG_CUDA(c.misc.ensure(64), "scan state allocation");
-  HG_CUDA(cudaMemset(c.misc.p, 0, 64), "scan state init");
+  for (Lane &L : c.lanes) {
+    HG_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "stream creation");
+    HG_CUDA(cudaEventCreateWithFlags(&L.ws_done, cudaEventDisableTiming), "event creation");
+    HG_CUDA(cudaStreamCreateWithFlags(&L.copy_stream, cudaStreamNonBlocking), "stream creation");
+    HG_CUDA(cudaEventCreateWithFlags(&L.copy_done, cudaEventDisableTiming), "event creation");
+    for (auto &op : L.slice_done)
+      for (cudaEvent_t &e : op) HG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event creation");
+    HG_CUDA(cudaStreamCreateWithFlags(&L.d2h_stream, cudaStreamNonBlocking), "stream creation");
+    HG_CUDA(cudaEventCreateWithFlags(&L.carry_done, cudaEventDisableTiming), "event creation");
+    HG_CUDA(cudaEventCreateWithFlags(&L.d2h_done, cudaEventDisableTiming), "event creation");
+    HG_CUDA(L.misc.ensure(64), "scan state allocation");
+    HG_CUDA(cudaMemset(L.misc.p, 0, 64), "scan state init");
+  }
+  c.lane = &c.lanes[0];
   c.ready = true;
   return HG_OK;
 }
@@ -409,7 +431,7 @@ PassArgs base_args(int L, int nops) {
     a.pc[i] = g_ctx.pc[i];
     a.tb[i] = g_ctx.tb[i];
   }
-  a.err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
+  a.err = err_word();
   return a;
 }
 
@@ -541,29 +563,29 @@ CrtConst crt_const(int L) {
 
 // Serialise use of the shared workspace across streams.
 cudaError_t ws_acquire(cudaStream_t st) {
-  if (g_ctx.ws_pending) return cudaStreamWaitEvent(st, g_ctx.ws_done, 0);
+  if (g_ctx.lane->ws_pending) return cudaStreamWaitEvent(st, g_ctx.lane->ws_done, 0);
   return cudaSuccess;
 }
 cudaError_t ws_release(cudaStream_t st) {
-  g_ctx.ws_pending = true;
-  return cudaEventRecord(g_ctx.ws_done, st);
+  g_ctx.lane->ws_pending = true;
+  return cudaEventRecord(g_ctx.lane->ws_done, st);
 }
 
 int scan_state(uint64_t tiles, ScanState *ss) {
   Context &c = g_ctx;
   const size_t need = (tiles + 1) * sizeof(unsigned long long);
-  if (need > c.flags.bytes) {
+  if (need > c.lane->flags.bytes) {
     HG_CUDA(cudaDeviceSynchronize(), "sync before flag growth");
-    HG_CUDA(c.flags.ensure(need * 2), "flag allocation");
-    HG_CUDA(cudaMemset(c.flags.p, 0, c.flags.bytes), "flag init");
+    HG_CUDA(c.lane->flags.ensure(need * 2), "flag allocation");
+    HG_CUDA(cudaMemset(c.lane->flags.p, 0, c.lane->flags.bytes), "flag init");
   }
-  if (++c.epoch == 0) c.epoch = 1;
-  ss->ticket = static_cast<unsigned long long *>(c.misc.p);
-  ss->ticket_base = c.ticket_count;
-  ss->flags = static_cast<unsigned long long *>(c.flags.p);
-  ss->epoch = c.epoch;
-  ss->err = reinterpret_cast<int *>(static_cast<char *>(c.misc.p) + 8);
-  c.ticket_count += tiles;
+  if (++c.lane->epoch == 0) c.lane->epoch = 1;
+  ss->ticket = static_cast<unsigned long long *>(c.lane->misc.p);
+  ss->ticket_base = c.lane->ticket_count;
+  ss->flags = static_cast<unsigned long long *>(c.lane->flags.p);
+  ss->epoch = c.lane->epoch;
+  ss->err = err_word();
+  c.lane->ticket_count += tiles;
   return HG_OK;
 }
 
@@ -638,23 +660,23 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   const uint64_t T = uint64_t(1) << L;
   const uint64_t slab = static_cast<uint64_t>(kPrimes) * T;
   HG_CUDA(ws_acquire(st), "workspace ordering");
-  if (c.A.bytes < cp.nchunks * slab * 8 || c.B.bytes < slab * 8) {
+  if (c.lane->A.bytes < cp.nchunks * slab * 8 || c.lane->B.bytes < slab * 8) {
     HG_CUDA(cudaDeviceSynchronize(), "sync before workspace growth");
-    HG_CUDA(c.A.ensure(cp.nchunks * slab * 8), "workspace allocation");
-    HG_CUDA(c.B.ensure(slab * 8), "workspace allocation");
+    HG_CUDA(c.lane->A.ensure(cp.nchunks * slab * 8), "workspace allocation");
+    HG_CUDA(c.lane->B.ensure(slab * 8), "workspace allocation");
   }
   const std::vector<PassPlan> plan = plan_passes(L);
   const bool one_pass = plan.size() == 1;
   PassArgs a = base_args(L, 1);  // the chunks
-  a.data[0] = c.A.u64();
-  a.data[1] = c.B.u64();
+  a.data[0] = c.lane->A.u64();
+  a.data[1] = c.lane->B.u64();
   a.limbs[0] = lng;
   a.nlimbs[0] = nl;
   a.chunk = cp.chunk;
   a.nprod = cp.nchunks;
   a.ws_stride = slab;
   PassArgs sp = base_args(L, 1);  // the short operand's spectrum
-  sp.data[0] = c.B.u64();
+  sp.data[0] = c.lane->B.u64();
   sp.limbs[0] = sht;
   sp.nlimbs[0] = ns;
   auto chunks_forward = [&]() -> int {
@@ -679,7 +701,7 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
     HG_CUDA(run_contig(m, plan.back(), kContigMulSpec, st), "middle pass");
   }
   PassArgs inv = base_args(L, 1);
-  inv.data[0] = c.A.u64();
+  inv.data[0] = c.lane->A.u64();
   inv.nprod = cp.nchunks;
   inv.ws_stride = slab;
   HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
@@ -691,7 +713,7 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   uint64_t tiles = 0;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(size), 2);  // local scan + fix
-    HG_CUDA(launch_crt_carry_chunks(c.A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L), out, size, ss, st,
+    HG_CUDA(launch_crt_carry_chunks(c.lane->A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L), out, size, ss, st,
                                     &tiles),
             "reconstruction");
   }
@@ -752,10 +774,10 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     if (host) {
       HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(x), host->hx, nx * 8, cudaMemcpyHostToDevice, st),
               "operand upload");
-      HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(y), host->hy, ny * 8, cudaMemcpyHostToDevice, c.copy_stream),
+      HG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(y), host->hy, ny * 8, cudaMemcpyHostToDevice, c.lane->copy_stream),
               "operand upload");
-      HG_CUDA(cudaEventRecord(c.copy_done, c.copy_stream), "operand upload");
-      y_ready = c.copy_done;
+      HG_CUDA(cudaEventRecord(c.lane->copy_done, c.lane->copy_stream), "operand upload");
+      y_ready = c.lane->copy_done;
     }
     return chunk_product_device(x, nx, y, ny, out, nout, cp, st, y_ready);
   }
@@ -765,17 +787,17 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   const uint64_t N = uint64_t(1) << L;
   const size_t words = static_cast<size_t>(kPrimes) * N;
   HG_CUDA(ws_acquire(st), "workspace ordering");
-  if (c.A.bytes < words * 8 || (!square && c.B.bytes < words * 8)) {
+  if (c.lane->A.bytes < words * 8 || (!square && c.lane->B.bytes < words * 8)) {
     HG_CUDA(cudaDeviceSynchronize(), "sync before workspace growth");
-    HG_CUDA(c.A.ensure(words * 8), "workspace allocation");
-    if (!square) HG_CUDA(c.B.ensure(words * 8), "workspace allocation");
+    HG_CUDA(c.lane->A.ensure(words * 8), "workspace allocation");
+    if (!square) HG_CUDA(c.lane->B.ensure(words * 8), "workspace allocation");
   }
   // Strided forward passes, the fused middle (last forward pass of both
   // operands + pointwise product + first inverse pass), strided inverse passes.
   const std::vector<PassPlan> plan = plan_passes(L);
   PassArgs a = base_args(L, square ? 1 : 2);
-  a.data[0] = c.A.u64();
-  a.data[1] = c.B.u64();
+  a.data[0] = c.lane->A.u64();
+  a.data[1] = c.lane->B.u64();
   a.limbs[0] = x;
   a.limbs[1] = square ? nullptr : y;
   a.nlimbs[0] = nx;
@@ -806,13 +828,13 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
       for (int k = 0; k < K; ++k) {
         const uint64_t t0 = ntiles * k / K, t1 = ntiles * (k + 1) / K;
         HG_CUDA(copy_columns(const_cast<uint64_t *>(op ? y : x), op ? host->hy : host->hx, op ? ny : nx, S, t0 * C,
-                             t1 * C, c.copy_stream),
+                             t1 * C, c.lane->copy_stream),
                 "operand upload");
-        HG_CUDA(cudaEventRecord(c.slice_done[op][k], c.copy_stream), "operand upload");
-        HG_CUDA(cudaStreamWaitEvent(st, c.slice_done[op][k], 0), "operand upload ordering");
+        HG_CUDA(cudaEventRecord(c.lane->slice_done[op][k], c.lane->copy_stream), "operand upload");
+        HG_CUDA(cudaStreamWaitEvent(st, c.lane->slice_done[op][k], 0), "operand upload ordering");
         PassArgs f = a;
         f.nops = 1;
-        f.data[0] = op ? c.B.u64() : c.A.u64();
+        f.data[0] = op ? c.lane->B.u64() : c.lane->A.u64();
         f.limbs[0] = op ? y : x;
         f.nlimbs[0] = op ? ny : nx;
         f.logR = p0.logR;
@@ -836,7 +858,7 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     HG_CUDA(run_contig(m, plan.back(), square ? kContigSqr : kContigMul, st), "middle pass");
   }
   PassArgs inv = base_args(L, 1);
-  inv.data[0] = c.A.u64();
+  inv.data[0] = c.lane->A.u64();
   HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
   if (nout > N) HG_CUDA(cudaMemsetAsync(out + N, 0, (nout - N) * sizeof(uint64_t), st), "zero tail");
   ScanState ss;
@@ -846,7 +868,7 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   uint64_t tiles = 0;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(nproc), 2);  // local scan + fix
-    HG_CUDA(launch_crt_carry(c.A.u64(), L, crt_const(L), out, nout, ss, st, &tiles), "reconstruction");
+    HG_CUDA(launch_crt_carry(c.lane->A.u64(), L, crt_const(L), out, nout, ss, st, &tiles), "reconstruction");
   }
   HG_CUDA(ws_release(st), "workspace ordering");
   return HG_OK;
@@ -948,7 +970,7 @@ int noalloc_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, ui
   ss.ticket_base = 0;
   ss.flags = reinterpret_cast<unsigned long long *>(scan + 1);
   ss.epoch = 1;
-  ss.err = reinterpret_cast<int *>(static_cast<char *>(c.misc.p) + 8);
+  ss.err = err_word();
   uint64_t used = 0;
   HG_CUDA(launch_crt_carry(scratch, L, crt_const(L), out, nout, ss, st, &used), "reconstruction");
   return HG_OK;
@@ -1004,7 +1026,7 @@ int read_checked_faults() {
 
 int read_device_error(cudaStream_t st) {
   int err = 0;
-  int *d_err = reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8);
+  int *d_err = err_word();
   HG_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st), "error word read");
   HG_CUDA(cudaStreamSynchronize(st), "stream synchronise");
 #if HG_CHECKED
@@ -1061,7 +1083,7 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
     return HG_OK;
   }
   const size_t nd = size;  // limbs computed on the device; the rest are zero
-  cudaStream_t st = c.stream;
+  cudaStream_t st = c.lane->stream;
   // Pinned (page-locked) host buffers are addressable from the device over
   // the host link, so the kernels read the operands and write the product
   // in place; pageable buffers go through device staging buffers.
@@ -1075,27 +1097,27 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
   const bool host_ops = (kind == Kind::Ntt || kind == Kind::Square) && ilog2_ceil(size) > kTileBits;
   const HostOperands ho{x, kind == Kind::Ntt ? y : nullptr};
   if (host_ops) {
-    HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
-    dx = c.X.u64();
+    HG_CUDA(c.lane->X.ensure(nx * 8), "operand allocation");
+    dx = c.lane->X.u64();
     if (kind == Kind::Ntt) {
-      HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
-      dy = c.Y.u64();
+      HG_CUDA(c.lane->Y.ensure(ny * 8), "operand allocation");
+      dy = c.lane->Y.u64();
     }
   }
   if (!dx) {
-    HG_CUDA(c.X.ensure(nx * 8), "operand allocation");
-    HG_CUDA(cudaMemcpyAsync(c.X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
-    dx = c.X.u64();
+    HG_CUDA(c.lane->X.ensure(nx * 8), "operand allocation");
+    HG_CUDA(cudaMemcpyAsync(c.lane->X.p, x, nx * 8, cudaMemcpyHostToDevice, st), "operand upload");
+    dx = c.lane->X.u64();
   }
   if (two && !dy) {
-    HG_CUDA(c.Y.ensure(ny * 8), "operand allocation");
-    HG_CUDA(cudaMemcpyAsync(c.Y.p, y, ny * 8, cudaMemcpyHostToDevice, st), "operand upload");
-    dy = c.Y.u64();
+    HG_CUDA(c.lane->Y.ensure(ny * 8), "operand allocation");
+    HG_CUDA(cudaMemcpyAsync(c.lane->Y.p, y, ny * 8, cudaMemcpyHostToDevice, st), "operand upload");
+    dy = c.lane->Y.u64();
   }
   const bool staged_out = (dout == nullptr);
   if (staged_out) {
-    HG_CUDA(c.OUT.ensure(nd * 8), "result allocation");
-    dout = c.OUT.u64();
+    HG_CUDA(c.lane->OUT.ensure(nd * 8), "result allocation");
+    dout = c.lane->OUT.u64();
   }
   switch (kind) {
     case Kind::Ntt: rc = ntt_product_device(dx, nx, dy, ny, dout, nd, st, host_ops ? &ho : nullptr); break;
@@ -1109,6 +1131,103 @@ int host_product(Kind kind, const uint64_t *x, size_t nx, const uint64_t *y, siz
   if (rc) return rc;
   if (nout > nd) memset(out + nd, 0, (nout - nd) * sizeof(uint64_t));
   return HG_OK;
+}
+
+// ---- many host-memory products, pipelined (hg_mul_host_pipeline) ----------
+//
+// Product i runs in lane i mod 2: its operands go up on the lane's copy
+// stream in column slices of the first pass (as in hg_mul), its transforms
+// and carry run on the lane's stream into the lane's device result buffer,
+// and a copy on the lane's download stream brings the result down.  While
+// product i's result goes down, product i + 1's operands go up and its
+// transforms run in the other lane; product i + 2 reuses lane i's buffers
+// once product i's download is done (its upload waits for product i's carry,
+// its carry for product i's download).
+
+struct TailZero {
+  uint64_t *p;
+  size_t n;
+};
+
+void CUDART_CB zero_tail(void *arg) {
+  TailZero *t = static_cast<TailZero *>(arg);
+  memset(t->p, 0, t->n * sizeof(uint64_t));
+  delete t;
+}
+
+int pipeline_one(Lane &L, const hg_host_product &q) {
+  const bool square = q.y == nullptr;
+  if (!q.out || (q.nx && !q.x) || (!square && q.ny && !q.y)) return fail(HG_ERR_ARG, "null pointer");
+  const size_t nx = trimmed(q.x, q.nx);
+  const size_t ny = square ? nx : trimmed(q.y, q.ny);
+  const size_t size = nx + ny;
+  if (q.nout < size) return fail(HG_ERR_ARG, "nout = %zu cannot hold the %zu-limb product", q.nout, size);
+  if (L.d2h_pending) {
+    HG_CUDA(cudaStreamWaitEvent(L.copy_stream, L.carry_done, 0), "lane ordering");
+    HG_CUDA(cudaStreamWaitEvent(L.stream, L.d2h_done, 0), "lane ordering");
+  }
+  size_t nd = 0;  // limbs computed on the device
+  if (nx && ny) {
+    if (ilog2_ceil(size) <= kTileBits) {  // one contiguous pass reads the operands: they go up on the stream
+      HG_CUDA(L.X.ensure(nx * 8), "operand allocation");
+      HG_CUDA(cudaMemcpyAsync(L.X.p, q.x, nx * 8, cudaMemcpyHostToDevice, L.stream), "operand upload");
+      if (!square) {
+        HG_CUDA(L.Y.ensure(ny * 8), "operand allocation");
+        HG_CUDA(cudaMemcpyAsync(L.Y.p, q.y, ny * 8, cudaMemcpyHostToDevice, L.stream), "operand upload");
+      }
+      HG_CUDA(L.OUT.ensure(size * 8), "result allocation");
+      const int rc = ntt_product_device(L.X.u64(), nx, square ? nullptr : L.Y.u64(), ny, L.OUT.u64(), size, L.stream);
+      if (rc) return rc;
+    } else {
+      HG_CUDA(L.X.ensure(nx * 8), "operand allocation");
+      if (!square) HG_CUDA(L.Y.ensure(ny * 8), "operand allocation");
+      HG_CUDA(L.OUT.ensure(size * 8), "result allocation");
+      const HostOperands ho{q.x, square ? nullptr : q.y};
+      const int rc = ntt_product_device(L.X.u64(), nx, square ? nullptr : L.Y.u64(), ny, L.OUT.u64(), size,
+                                        L.stream, &ho);
+      if (rc) return rc;
+    }
+    nd = size;
+  }
+  HG_CUDA(cudaEventRecord(L.carry_done, L.stream), "lane ordering");
+  HG_CUDA(cudaStreamWaitEvent(L.d2h_stream, L.carry_done, 0), "lane ordering");
+  if (nd) HG_CUDA(cudaMemcpyAsync(q.out, L.OUT.p, nd * 8, cudaMemcpyDeviceToHost, L.d2h_stream), "result download");
+  if (q.nout > nd) {
+    TailZero *t = new TailZero{q.out + nd, q.nout - nd};
+    const cudaError_t e = cudaLaunchHostFunc(L.d2h_stream, zero_tail, t);
+    if (e != cudaSuccess) {
+      delete t;
+      return cuda_fail(e, "result tail");
+    }
+  }
+  HG_CUDA(cudaEventRecord(L.d2h_done, L.d2h_stream), "lane ordering");
+  L.d2h_pending = true;
+  return HG_OK;
+}
+
+int host_pipeline(const hg_host_product *prods, size_t n) {
+  std::lock_guard<std::recursive_mutex> lock(g_ctx.mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (n && !prods) return fail(HG_ERR_ARG, "null pointer");
+  Context &c = g_ctx;
+  for (size_t i = 0; i < n && rc == HG_OK; ++i) {
+    c.lane = &c.lanes[i % kLanes];
+    rc = pipeline_one(*c.lane, prods[i]);
+  }
+  c.lane = &c.lanes[0];
+  // Nothing of this call may still write into the caller's buffers after it returns.
+  for (Lane &L : c.lanes) {
+    if (!L.d2h_pending) continue;
+    const cudaError_t e = cudaStreamSynchronize(L.d2h_stream);
+    if (e != cudaSuccess && rc == HG_OK) rc = cuda_fail(e, "result download");
+    L.d2h_pending = false;
+  }
+  if (rc) {
+    cudaDeviceSynchronize();
+    return rc;
+  }
+  return read_device_error(c.lanes[0].stream);
 }
 
 int spectrum(uint64_t *a, size_t n, int mod_num, bool inverse, cudaStream_t st) {
@@ -1242,7 +1361,7 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
 BatchBufs batch_bufs(hg_batch *b) {
   return BatchBufs{static_cast<const ProductDesc *>(b->d_desc.p), b->ws.u64(),
                    static_cast<unsigned long long *>(b->flags.p), static_cast<unsigned long long *>(b->tickets.p),
-                   reinterpret_cast<int *>(static_cast<char *>(g_ctx.misc.p) + 8)};
+                   err_word()};
 }
 
 // ---- the persistent schedule (hg_persist.cu) -------------------------------
@@ -1385,7 +1504,7 @@ int persist_build(hg_batch *b) {
   std::vector<PersistPhase> indep;  // zeroing: waits for nothing
   for (size_t gi = 0; gi < bp.groups.size(); ++gi) {
     const BatchGroup &g = bp.groups[gi];
-    per.push_back(group_phases(g, bb, bb.ws + l.ws_off[gi], bb.flags + l.flag_off[gi], g_ctx.stream));
+    per.push_back(group_phases(g, bb, bb.ws + l.ws_off[gi], bb.flags + l.flag_off[gi], g_ctx.lane->stream));
     if (g.tails) {
       PersistPhase z{};
       z.kind = kPhaseZero;
@@ -1459,7 +1578,7 @@ int batch_clear_scan(const BatchPlan &bp, const BatchBufs &bb, cudaStream_t st) 
 // Time each candidate schedule of each group (twice; the second run counts)
 // and keep the fastest.
 int batch_autotune(hg_batch *b) {
-  cudaStream_t st = g_ctx.stream;
+  cudaStream_t st = g_ctx.lane->stream;
   cudaEvent_t e0, e1;
   HG_CUDA(cudaEventCreate(&e0), "event creation");
   HG_CUDA(cudaEventCreate(&e1), "event creation");
@@ -1508,7 +1627,7 @@ int batch_autotune(hg_batch *b) {
 // Time the whole batch on both schedules (twice each; the second run
 // counts) and keep the faster.
 int schedule_autotune(hg_batch *b) {
-  cudaStream_t st = g_ctx.stream;
+  cudaStream_t st = g_ctx.lane->stream;
   cudaEvent_t e0, e1;
   HG_CUDA(cudaEventCreate(&e0), "event creation");
   HG_CUDA(cudaEventCreate(&e1), "event creation");
@@ -1692,7 +1811,7 @@ int large_sum_device(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t 
   ScanState ss;
   rc = scan_state(carry_tiles(nproc), &ss);
   if (rc) return rc;
-  long long *top = reinterpret_cast<long long *>(static_cast<char *>(g_ctx.misc.p) + 16);
+  long long *top = reinterpret_cast<long long *>(static_cast<char *>(g_ctx.lane->misc.p) + 16);
   {
     // (top search,) local scan, fix, sign and size
     ProfScope ps(HG_KC_OTHER, st, 24.0 * static_cast<double>(nproc), sa != sb ? 4 : 3);
@@ -1798,29 +1917,34 @@ int hg_shutdown(void) {
   if (!c.ready) return HG_OK;
   if (g_services.load() > 0) return fail(HG_ERR_ARG, "close every multiply service before hg_shutdown");
   cudaDeviceSynchronize();
-  c.A.release();
-  c.B.release();
-  c.X.release();
-  c.Y.release();
-  c.OUT.release();
-  c.flags.release();
-  c.misc.release();
+  for (Lane &L : c.lanes) {
+    L.A.release();
+    L.B.release();
+    L.X.release();
+    L.Y.release();
+    L.OUT.release();
+    L.flags.release();
+    L.misc.release();
+    for (cudaStream_t *st : {&L.stream, &L.copy_stream, &L.d2h_stream}) {
+      if (*st) cudaStreamDestroy(*st);
+      *st = nullptr;
+    }
+    for (cudaEvent_t *e : {&L.ws_done, &L.copy_done, &L.carry_done, &L.d2h_done}) {
+      if (*e) cudaEventDestroy(*e);
+      *e = nullptr;
+    }
+    for (auto &op : L.slice_done)
+      for (cudaEvent_t &e : op) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+      }
+    L.ws_pending = L.d2h_pending = false;
+    L.ticket_count = 0;
+    L.epoch = 0;
+  }
+  c.lane = &c.lanes[0];
   c.tables.release();
   release_pass_twiddles();
-  if (c.stream) cudaStreamDestroy(c.stream);
-  if (c.ws_done) cudaEventDestroy(c.ws_done);
-  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
-  if (c.copy_done) cudaEventDestroy(c.copy_done);
-  for (auto &op : c.slice_done)
-    for (cudaEvent_t &e : op) {
-      if (e) cudaEventDestroy(e);
-      e = nullptr;
-    }
-  c.stream = nullptr;
-  c.ws_done = nullptr;
-  c.copy_stream = nullptr;
-  c.copy_done = nullptr;
-  c.ws_pending = false;
   c.ready = false;
   // The scratch array's device address belongs to the module as loaded in
   // the current context: after a context reset the module loads again, so
@@ -1861,6 +1985,8 @@ int hg_chunk_plan(size_t nx, size_t ny, int *log_len, size_t *chunk, size_t *nch
 }
 
 int hg_set_chunking(int enable) { return hg::g_chunking.exchange(enable ? 1 : 0); }
+
+int hg_mul_host_pipeline(const hg_host_product *prods, size_t n) { return host_pipeline(prods, n); }
 
 int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t *out, size_t nout) {
   return host_product(Kind::Ntt, x, nx, y, ny, 0, out, nout);
@@ -1964,7 +2090,7 @@ int hg_sync(void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!st) {
     HG_CUDA(cudaDeviceSynchronize(), "device synchronise");
-    st = g_ctx.stream;
+    st = g_ctx.lane->stream;
   }
   return read_device_error(st);
 }

@@ -129,6 +129,30 @@ def mpz_square(x: MPZ) -> MPZ:
     return MPZ(1, out)
 
 
+def mul_host_pipeline(items) -> None:
+    """Many NTT products of host arrays in one pipelined call
+    (hg_mul_host_pipeline): items are (x, y_or_None, out) uint64 arrays (or
+    pinned torch tensors, via .data_ptr()); out receives |x| * |y| (|x|^2
+    when y is None) and zeros to its end.  Outputs shared by products must be
+    at least two apart in the list."""
+    from ._lib import HgHostProduct
+
+    arr = (HgHostProduct * len(items))()
+    keep = []
+    for k, (x, y, out) in enumerate(items):
+        def addr(a):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                return a.data_ptr()
+            keep.append(a)
+            return a.ctypes.data
+
+        n = (lambda a: 0 if a is None else (a.numel() if hasattr(a, "numel") else len(a)))
+        arr[k] = HgHostProduct(addr(x), n(x), addr(y), n(y), addr(out), n(out))
+    check(load().hg_mul_host_pipeline(arr, len(items)))
+
+
 def multiply_storage_schoolboy(a: np.ndarray, a_size: int, b: np.ndarray, b_size: int) -> np.ndarray:
     """%multiply-storage/schoolboy (src/mpz-ram.lisp:404-431): storage of
     1 + a_size + b_size digits."""

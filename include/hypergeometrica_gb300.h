@@ -119,6 +119,26 @@ int hg_mul(const uint64_t *x, size_t nx, const uint64_t *y, size_t ny, uint64_t 
 /* mpz-square (src/ntt-multiply.lisp:101-172): |x|^2. */
 int hg_sqr(const uint64_t *x, size_t nx, uint64_t *out, size_t nout);
 
+/* Many NTT products or squares (mpz-*-ntt and mpz-square, src/ntt-multiply.lisp:101-254) on
+ * host memory in one call, pipelined: while one product's result is copied
+ * down, the next product's operands go up and its transforms run, in a
+ * second set of device buffers.  Each product is computed exactly as hg_mul
+ * (hg_sqr when y is NULL) computes it; out receives the product and zeros
+ * up to nout.  Returns once every result is in host memory.  The copies
+ * overlap only for page-locked (pinned) buffers.  Products that share an
+ * output buffer must be at least two apart in the list (products two apart
+ * are written in list order); the first product of a new size allocates
+ * that size's device buffers. */
+typedef struct hg_host_product {
+    const uint64_t *x; /* host limbs                          */
+    size_t nx;
+    const uint64_t *y; /* host limbs; NULL squares x          */
+    size_t ny;
+    uint64_t *out;     /* host result, nout >= nx + ny limbs (2nx square) */
+    size_t nout;
+} hg_host_product;
+int hg_mul_host_pipeline(const hg_host_product *prods, size_t n);
+
 /* %multiply-storage/schoolboy (src/mpz-ram.lisp:404-431): |x| * |y| by the
  * quadratic method, used by mpz-* when the smaller operand has at most
  * *ntt-multiply-threshold* limbs (src/multiply.lisp:37-42). */
