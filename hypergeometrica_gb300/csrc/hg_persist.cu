@@ -50,21 +50,31 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 
 // Each kind of item is a separate (not inlined) function, so that ptxas
 // allocates registers per body rather than across all of them at once.
+template <int LOGR, bool INV>
+__device__ __noinline__ void run_strided_dir(const PassArgs &P, uint64_t item, ulonglong2 *tw, uint64_t *sm) {
+  strided_ldg_body<LOGR, INV>(P, item, tw, sm);
+}
+
 template <int LOGR>
-__device__ __noinline__ void run_strided(const PassArgs &P, bool inv, uint64_t item, ulonglong2 *tw,
+__device__ __forceinline__ void run_strided(const PassArgs &P, bool inv, uint64_t item, ulonglong2 *tw,
                                             uint64_t *sm) {
   if (inv)
-    strided_ldg_body<LOGR, true>(P, item, tw, sm);
+    run_strided_dir<LOGR, true>(P, item, tw, sm);
   else
-    strided_ldg_body<LOGR, false>(P, item, tw, sm);
+    run_strided_dir<LOGR, false>(P, item, tw, sm);
+}
+
+template <int T, int MODE>
+__device__ __noinline__ void run_contig_mode(const PassArgs &P, uint64_t bx, int by, uint64_t *sm) {
+  contig_body<T, MODE>(P, bx, by, sm);
 }
 
 template <int T>
-__device__ __noinline__ void run_contig(const PassArgs &P, int mode, uint64_t bx, int by, uint64_t *sm) {
+__device__ __forceinline__ void run_contig(const PassArgs &P, int mode, uint64_t bx, int by, uint64_t *sm) {
   if (mode == kMul)
-    contig_body<T, kMul>(P, bx, by, sm);
+    run_contig_mode<T, kMul>(P, bx, by, sm);
   else
-    contig_body<T, kSqr>(P, bx, by, sm);
+    run_contig_mode<T, kSqr>(P, bx, by, sm);
 }
 
 __device__ __noinline__ void run_tiny(const PersistPhase &ph, uint64_t item) {
