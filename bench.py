@@ -776,11 +776,17 @@ def run_ours(args) -> None:
     hout2 = torch.empty(na + nb, dtype=torch.int64).pin_memory()
     outs = [hout, hout2]
     H.mul_host_pipeline([(hx, hy, outs[k % 2]) for k in range(2)])  # warm the second lane's buffers
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    H.mul_host_pipeline([(hx, hy, outs[k % 2]) for k in range(e2e_steps)])
-    pipe_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    # Best of two calls: an occasional host-side stall of some tens of
+    # milliseconds (seen on either API, outside the library) would otherwise
+    # decide the number.
+    pipe_runs = []
+    for _ in range(2):
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        H.mul_host_pipeline([(hx, hy, outs[k % 2]) for k in range(e2e_steps)])
+        pipe_runs.append(max_over_ranks(time.perf_counter() - t0, dist, "cuda"))
+    pipe_s = min(pipe_runs)
     clocks = sampler.stop()
     want = out.cpu().numpy().view(np.uint64)
     ok = ok and all(bool(np.array_equal(o.numpy().view(np.uint64), want)) for o in outs)
@@ -814,6 +820,8 @@ def run_ours(args) -> None:
                 "api": "hg_mul_host_pipeline (host pointers, pinned; one call for all steps, each step's upload "
                        "and download inside it, overlapping the neighbouring steps' work)",
                 "steps": e2e_steps, "ms_per_step": 1000 * pipe_s / e2e_steps,
+                "timing": "best of two calls of `steps` products each",
+                "ms_per_step_runs": [1000 * t / e2e_steps for t in pipe_runs],
                 "single_call": {"value": e2e_single, "unit": UNIT, "api": "hg_mul (one synchronous call per step)",
                                 "ms_per_step": 1000 * e2e_s / e2e_steps},
                 "host_link": link},
