@@ -632,11 +632,21 @@ def run_expt() -> dict:
             "reference_published_s": 136.233, "reference_published_note": "logs/24apr21-999-ram.txt, other hardware"}
 
 
-def _int_roofline(N: int, ms_per_product: float) -> dict:
+# Thread instructions per radix-2 butterfly of the middle kernel (ncu,
+# profiles/ntt_contig_mul_2e22.md): the fewest any pass of the product spends.
+INSTR_PER_BUTTERFLY = 33.8
+
+
+def _int_roofline(N: int, ms_per_product: float, sm_mhz) -> dict:
     """The product's radix-2 butterflies (3 primes x 3 transforms x N/2 log2 N)
-    per second against hg_butterfly_peak: a memory-free network of the same
-    modular butterflies over every SM, measured now."""
+    per second against two ceilings: hg_butterfly_peak, a memory-free network
+    of the same modular butterflies over every SM measured now, and the
+    issue-rate floor, every SM sub-partition issuing one warp instruction
+    per clock at the clock sampled under load, with the middle kernel's
+    33.8 thread instructions per butterfly."""
     import ctypes
+
+    import torch
 
     from hypergeometrica_gb300 import _lib
 
@@ -644,9 +654,15 @@ def _int_roofline(N: int, ms_per_product: float) -> dict:
     _lib.check(_lib.load().hg_butterfly_peak(ctypes.byref(pk)))
     bf = 3 * 3 * (N // 2) * (N.bit_length() - 1)
     achieved = bf / (ms_per_product / 1000.0)
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    issue = sms * 4 * mhz * 1e6 * 32 / INSTR_PER_BUTTERFLY
     return {"bound": "int-pipe", "butterflies_per_product": bf, "achieved": achieved, "peak": pk.value,
             "unit": "butterflies/s", "frac": achieved / pk.value,
-            "peak_source": "hg_butterfly_peak (register-only network of the same butterflies)"}
+            "peak_source": "hg_butterfly_peak (register-only network of the same butterflies)",
+            "issue_floor": {"peak": issue, "frac": achieved / issue, "sms": sms, "sm_mhz": mhz,
+                            "thread_instructions_per_butterfly": INSTR_PER_BUTTERFLY,
+                            "source": "one warp instruction per clock per SM sub-partition (4 per SM)"}}
 
 
 def host_link(nbytes: int = 256 << 20) -> dict:
@@ -831,7 +847,7 @@ def run_ours(args) -> None:
                      "launches": d["launches"], "ms_per_launch": d["ms"] / max(1, d["launches"])},
         "roofline_product": {"algorithmic_bytes": b_mul, "achieved": prod_gbs, "frac": prod_gbs / peak,
                              "unit": "GB/s", "formula": "16(na+nb) + 192 N"},
-        "roofline_int": _int_roofline(N, ms / args.steps),
+        "roofline_int": _int_roofline(N, ms / args.steps, clocks["sm_mhz"]),
         "kernels": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof.items() if v["launches"]},
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"],
                    "samples": clocks["samples"]},
