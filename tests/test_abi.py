@@ -94,6 +94,8 @@ def test_no_cpu_fallback_without_gpu(lib):
     a = np.ones(4, dtype=np.uint64)
     out = np.zeros(8, dtype=np.uint64)
     assert lib.hg_mul(a.ctypes.data, 4, a.ctypes.data, 4, out.ctypes.data, 8) != 0
+    with pytest.raises(H.HGError):
+        H.mul_host_pipeline([(a, a, out), (a, None, out.copy())])
 
 
 def _scheme_roots(oracle, maxlg):

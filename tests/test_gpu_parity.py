@@ -342,3 +342,37 @@ def test_error_behaviour(hg):
     x = hg.MPZ.from_int(0)
     assert hg.mpz_mul(x, hg.MPZ.from_int(5)).to_int() == 0
     assert int_from_digits(digits_from_int(0)) == 0
+
+
+def test_unaligned_device_arrays(hg, oracle):
+    """Arrays at an 8-byte offset from a 16-byte boundary (a slice one limb
+    into a tensor) cannot be staged by TMA; those passes run with per-thread
+    loads and stores and give the same limbs and spectra."""
+    from hypergeometrica_gb300 import device as D
+
+    torch = _torch()
+    nx, ny = 300001, 200003
+    x = W.limbs(31, nx)
+    y = W.limbs(32, ny)
+    want = hg.mpz_mul_ntt(hg.MPZ(1, x), hg.MPZ(1, y)).storage
+    bx = torch.zeros(nx + 1, dtype=torch.int64, device="cuda")
+    by = torch.zeros(ny + 1, dtype=torch.int64, device="cuda")
+    bx[1:] = _dev(x)
+    by[1:] = _dev(y)
+    bo = torch.full((len(want) + 1,), -1, dtype=torch.int64, device="cuda")
+    tx, ty, out = bx[1:], by[1:], bo[1:]
+    assert tx.data_ptr() % 16 == 8 and out.data_ptr() % 16 == 8
+    D.mul(tx, ty, out)
+    D.sync()
+    assert np.array_equal(_host(out), want)
+    for lg in (13, 17):
+        v = W.splitmix64(lg + 90, 1 << lg) % np.uint64(oracle.moduli()[2])
+        buf = torch.zeros((1 << lg) + 1, dtype=torch.int64, device="cuda")
+        buf[1:] = _dev(v)
+        t = buf[1:]
+        D.ntt_forward(t, 2)
+        D.sync()
+        assert np.array_equal(_host(t), oracle.ntt_forward(v, 2)), lg
+        D.ntt_reverse(t, 2)
+        D.sync()
+        assert np.array_equal(_host(t), v), lg
