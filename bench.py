@@ -58,6 +58,21 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _pipes(kernel_class: str):
+    """Pipe utilisation of a kernel class from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 8 and parts[0] == "pipe_pct" and parts[1] == kernel_class:
+                    return {parts[2] + "_pct": float(parts[3]), parts[4] + "_pct": float(parts[5]),
+                            parts[6] + "_pct": float(parts[7]), "source": "profiles/ntt_contig_mul_2e22.md (ncu)"}
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def _traffic(kernel_class: str):
     """Per-launch DRAM bytes of a kernel class from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
@@ -844,7 +859,8 @@ def run_ours(args) -> None:
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": d["bytes"] / max(1, d["launches"]),
-                     "launches": d["launches"], "ms_per_launch": d["ms"] / max(1, d["launches"])},
+                     "launches": d["launches"], "ms_per_launch": d["ms"] / max(1, d["launches"]),
+                     "pipes": _pipes(dom)},
         "roofline_product": {"algorithmic_bytes": b_mul, "achieved": prod_gbs, "frac": prod_gbs / peak,
                              "unit": "GB/s", "formula": "16(na+nb) + 192 N"},
         "roofline_int": _int_roofline(N, ms / args.steps, clocks["sm_mhz"]),
