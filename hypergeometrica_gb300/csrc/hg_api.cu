@@ -824,7 +824,7 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
     // back on the copy stream.  From pageable memory the driver returns only
     // once a copy is staged, so the host stages slice k + 1 while the device
     // runs the pass on slice k (2^24 x 2^24 limbs: 9.30 -> 8.15 ms end to end).
-    for (int op = 0; op < nops; ++op)
+    for (int op = 0; op < nops; ++op) {
       for (int k = 0; k < K; ++k) {
         const uint64_t t0 = ntiles * k / K, t1 = ntiles * (k + 1) / K;
         HG_CUDA(copy_columns(const_cast<uint64_t *>(op ? y : x), op ? host->hy : host->hx, op ? ny : nx, S, t0 * C,
@@ -846,9 +846,15 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
         ProfScope ps(HG_KC_NTT_FORWARD, st, pass_bytes(f, 1, 1) * static_cast<double>(t1 - t0) / ntiles);
         HG_CUDA(launch_ntt_strided(f, false, st), "forward transform");
       }
-    PassArgs rest = a;
-    rest.limbs[0] = rest.limbs[1] = nullptr;
-    HG_CUDA(run_strided_range(rest, plan, false, 1, static_cast<int>(plan.size()) - 1, st), "forward transform");
+      // This operand's remaining strided passes run while the next one's
+      // upload lands (2^24 x 2^24 end to end: 7.29 -> 7.25 ms).
+      PassArgs rest = a;
+      rest.nops = 1;
+      rest.data[0] = op ? c.lane->B.u64() : c.lane->A.u64();
+      rest.limbs[0] = rest.limbs[1] = nullptr;
+      rest.nlimbs[0] = rest.nlimbs[1] = 0;
+      HG_CUDA(run_strided_range(rest, plan, false, 1, static_cast<int>(plan.size()) - 1, st), "forward transform");
+    }
   } else {
     HG_CUDA(run_strided(a, plan, false, st), "forward transform");
   }
