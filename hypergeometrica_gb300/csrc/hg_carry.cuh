@@ -119,11 +119,12 @@ __device__ __forceinline__ unsigned long long flag_word(uint32_t epoch, uint32_t
   return (static_cast<unsigned long long>(epoch) << 32) | (p << 3) | (g << 2) | 1u;
 }
 
-// One tile of 4096 output limbs per CTA, in ticket order.  Batch (batch !=
-// nullptr): tickets run product-major, tpp tiles per product; product k's
+// One tile of NT * 8 output limbs per CTA (tile gt).  Batch (batch !=
+// nullptr): tiles run product-major, tpp tiles per product; product k's
 // residues are rebased by k * ws_stride and its output is
-// batch[k].out[0, min(nout, n)).  Tiles of 4096 limbs, two 512-thread CTAs
-// per SM (64 registers).
+// batch[k].out[0, min(nout, n)).  The per-launch carry runs 256-thread
+// CTAs (2048-limb tiles), four per SM at 64 registers, as does the
+// persistent batch kernel.
 //
 // Each tile is written as if its carry-in were 0 and publishes its
 // aggregate (g, p) once; carry_fix_kernel, launched next on the same
