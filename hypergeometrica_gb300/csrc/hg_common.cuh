@@ -226,10 +226,34 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
 // Shoup product a * w mod p for any 64-bit a, w < p with companion
 // wq = floor(w * 2^64 / p) (the reference's m*/fast2,
 // src/modular-arithmetic.lisp:207-231).  q = floor(a * wq / 2^64) leaves
-// r = a*w - q*p in [0, 2p); q*p mod 2^64 is q + ((q * c) mod 2^9) * 2^55.
+// r = a*w - q*p in [0, 2p).  r is formed as a*w + q*(2^64 - p) mod 2^64 by
+// one chain of 32-bit multiply-adds (mul.wide, mad.wide, four mad.lo) on the
+// FMA pipe, none on the integer ALU pipe that the butterflies' additions and
+// selects keep busy.  The words of 2^64 - p come from p at run time, so the
+// compiler keeps them as multiplications.  On a register-only butterfly
+// network: 3-7% more forward and 2% more inverse butterflies per second than
+// subtracting q*p mod 2^64 = q + ((q * c) mod 2^9) * 2^55 on the ALU pipe
+// (the fold's subtraction and the additions moved onto IMAD measured slower).
 __device__ __forceinline__ uint64_t shoup_mul(uint64_t a, uint64_t w, uint64_t wq, uint64_t p, uint32_t c) {
+  (void)c;
   const uint64_t q = mul_hi64(a, wq);
-  const uint64_t r = a * w - q - (static_cast<uint64_t>(static_cast<uint32_t>(q) * (c << 23)) << 32);
+  const uint64_t np = 0 - p;
+  uint64_t r;
+  asm("{\n\t.reg .u32 a0, a1, w0, w1, q0, q1, n0, n1, r0, r1;\n\t"
+      "mov.b64 {a0, a1}, %1;\n\t"
+      "mov.b64 {w0, w1}, %2;\n\t"
+      "mov.b64 {q0, q1}, %3;\n\t"
+      "mov.b64 {n0, n1}, %4;\n\t"
+      "mul.wide.u32 %0, a0, w0;\n\t"
+      "mad.wide.u32 %0, q0, n0, %0;\n\t"
+      "mov.b64 {r0, r1}, %0;\n\t"
+      "mad.lo.u32 r1, a0, w1, r1;\n\t"
+      "mad.lo.u32 r1, a1, w0, r1;\n\t"
+      "mad.lo.u32 r1, q0, n1, r1;\n\t"
+      "mad.lo.u32 r1, q1, n0, r1;\n\t"
+      "mov.b64 %0, {r0, r1};\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(w), "l"(q), "l"(np));
   const uint64_t out = fold_p(r, p);
 #if HG_CHECKED
   if (out != mulmod_exact(a, w, p)) checked_fault(kDevProduct);
