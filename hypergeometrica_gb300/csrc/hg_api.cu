@@ -228,12 +228,8 @@ int cuda_fail(cudaError_t e, const char *what) {
 constexpr size_t kSubEntries = 2048;           // (w, companion) pairs per direction
 constexpr size_t kSubWords = 2 * kSubEntries;  // words per direction
 constexpr size_t kLevelWords = size_t(1) << kTwLevelBits;
-constexpr size_t kSwzWords = 2 * 2 * kSwzInverse;  // both directions, (w, companion) pairs
+constexpr size_t kSwzWords = 2 * 2 * kTwInverse;  // both directions, (w, companion) pairs
 constexpr size_t kPrimeTableWords = 2 * kSubWords + 4 * kLevelWords + kSwzWords;
-
-// The XOR swizzle of the contiguous pass's twiddle tables (swz_tw in
-// hg_ntt_rounds.cuh), on the host.
-uint32_t swz_tw_h(uint32_t e) { return e ^ ((e >> 3) & 7u) ^ ((e >> 6) & 7u) ^ ((e >> 9) & 7u); }
 
 // Shoup companion floor(w * 2^64 / p) (calc-b-inv, src/modular-arithmetic.lisp:207-208).
 uint64_t shoup_h(uint64_t w, uint64_t p) { return static_cast<uint64_t>(((u128)w << 64) / p); }
@@ -328,21 +324,21 @@ int init_locked(const uint64_t *moduli, int k, const uint64_t *roots, int maxlg,
       hi = mulmod_h(hi, step_i, p);
     }
   }
-  // Per block size 2^T, the sub-transform tables in swizzled order, copied
-  // from the 4096-point tables above (entry e of the table of T is entry
-  // e * 2^(12 - T) of the 4096-point one).
+  // Per block size 2^T, the sub-transform tables in padded (tw_pos) order,
+  // copied from the 4096-point tables above (entry e of the table of T is
+  // entry e * 2^(12 - T) of the 4096-point one); gap entries stay zero.
   for (int i = 0; i < kPrimes; ++i) {
     uint64_t *t = host.data() + i * kPrimeTableWords;
     const uint64_t *sub_f = t, *sub_i = t + kSubWords;
     uint64_t *swz = t + 2 * kSubWords + 4 * kLevelWords;
     for (int T = 1; T <= kTileBits; ++T) {
-      const uint32_t base = (1u << (T - 1)) - 1u;
+      const uint32_t base = tw_base(T);
       for (uint32_t e = 0; e < (1u << (T - 1)); ++e) {
-        const uint32_t src = e << (kTileBits - T), dst = base + swz_tw_h(e);
+        const uint32_t src = e << (kTileBits - T), dst = base + tw_pos(e);
         swz[2 * dst] = sub_f[2 * src];
         swz[2 * dst + 1] = sub_f[2 * src + 1];
-        swz[2 * (kSwzInverse + dst)] = sub_i[2 * src];
-        swz[2 * (kSwzInverse + dst) + 1] = sub_i[2 * src + 1];
+        swz[2 * (kTwInverse + dst)] = sub_i[2 * src];
+        swz[2 * (kTwInverse + dst) + 1] = sub_i[2 * src + 1];
       }
     }
   }

@@ -171,7 +171,7 @@ __device__ __forceinline__ void round_g(uint64_t (&v)[16], const ulonglong2 *tw,
   constexpr int NB = Gr::template NB<g>();
   constexpr int JG = Gr::template JG<g>();
   constexpr bool TZERO = (g == 0) && (A == 0) && (JG == 0);
-  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO, EDGE && TZERO>(v, tw, xt, p, c);
+  stages<NB, JG, A, 0, 4 * g, T, INV, TZERO, EDGE && TZERO, false, true>(v, tw, xt, p, c);
 }
 
 // Move the thread's registers from the layout of group g to that of group h
@@ -182,10 +182,10 @@ __device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_
   constexpr int Ag = Gr::template A<g>(), Ah = Gr::template A<h>();
   if constexpr (Ag == Ah) return;
   __syncthreads();
-  to_smem<Ag>(sm, v, xt);
+  to_smem<Ag, true>(sm, v, xt);
   __syncthreads();
   xt = thread_base<Ah>(tid);
-  from_smem<Ah>(v, sm, xt);
+  from_smem<Ah, true>(v, sm, xt);
 }
 
 // All forward rounds, from the top group down to group 0.
