@@ -239,7 +239,7 @@ __device__ __forceinline__ void load_block(uint64_t (&v)[16], const uint64_t *da
   } else {
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      v[i] = data[base + (xt | (static_cast<uint32_t>(i) << A))];
+      v[i] = ld_once(data + base + (xt | (static_cast<uint32_t>(i) << A)));
       check_below(v[i], bound ? bound : p);
     }
   }
