@@ -165,13 +165,24 @@ __global__ void __launch_bounds__(kTileThreads, 4)
       const uint64_t *lp = op ? L.limbs[1] : L.limbs[0];
       const uint64_t row0 = static_cast<uint64_t>(blk) << LOGR;
       const bool has_tail = tail != 0 && tr >= row0 && tr < row0 + (1u << LOGR);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
+      auto limb = [&](int i) {
         const uint32_t x = xt | (static_cast<uint32_t>(i) << AL);
         uint64_t w = tile[x];
         if (has_tail && row0 + (x >> ROWOFF) == tr && s0 + (x & ((1u << LOGTC) - 1u)) < tail)
           w = __ldg(lp + tr * (uint64_t(1) << logS) + s0 + (x & ((1u << LOGTC) - 1u)));
-        v[i] = reduce64(w, p);
+        return reduce64(w, p);
+      };
+      if (G == 2 && ((L.ztop >> op) & 1)) {
+        // Registers 8..15 hold the top row bit's upper half, past the limbs:
+        // zeros that the first stage (ZTOP) never reads, so neither read nor
+        // reduced here.
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = limb(i);
+        if constexpr (G == 2) stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false, false, true>(v, tw, xt, p, c);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = limb(i);
+        if constexpr (G == 2) stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false>(v, tw, xt, p, c);
       }
     } else {
 #pragma unroll
@@ -181,10 +192,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
       }
     }
     if constexpr (G == 2) {
-      if (LIMBS && ((L.ztop >> op) & 1))
-        stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false, false, true>(v, tw, xt, p, c);
-      else
-        stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false>(v, tw, xt, p, c);
+      if constexpr (!LIMBS) stages<NB1, 4 - NB1, A1, ROWOFF, 4, LOGR, false, false>(v, tw, xt, p, c);
       __syncthreads();  // every thread has its values out of the tile
       to_smem<A1>(tile, v, xt);
       __syncthreads();
