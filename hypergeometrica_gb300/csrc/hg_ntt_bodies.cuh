@@ -175,33 +175,45 @@ __device__ __forceinline__ void round_g(uint64_t (&v)[16], const ulonglong2 *tw,
 }
 
 // Move the thread's registers from the layout of group g to that of group h
-// through sm (two barriers: the buffer may still be read by the last round).
+// through sm.  The barrier after the writes makes them visible; the one
+// before them (wait) keeps the writes from overtaking threads that still
+// read the buffer's last exchange, and is left out where no thread has read
+// the buffer since the last barrier the whole CTA passed.
 template <int T, int g, int h>
-__device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_t &xt, uint32_t tid) {
+__device__ __forceinline__ void regroup(uint64_t (&v)[16], uint64_t *sm, uint32_t &xt, uint32_t tid,
+                                        bool wait = true) {
   using Gr = Groups<T>;
   constexpr int Ag = Gr::template A<g>(), Ah = Gr::template A<h>();
   if constexpr (Ag == Ah) return;
-  __syncthreads();
+  if (wait) __syncthreads();
   to_smem<Ag, true>(sm, v, xt);
   __syncthreads();
   xt = thread_base<Ah>(tid);
   from_smem<Ah, true>(v, sm, xt);
 }
 
+// Exchange buffers of a block's rounds: the first exchange goes through sm1,
+// the second (three groups) through sm2; wait1 and wait2 as regroup's wait.
+struct Exchanges {
+  uint64_t *sm1, *sm2;
+  bool wait1, wait2;
+};
+__device__ __forceinline__ Exchanges through(uint64_t *sm) { return Exchanges{sm, sm, true, true}; }
+
 // All forward rounds, from the top group down to group 0.
 template <int T>
-__device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
+__device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], Exchanges x, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
   if constexpr (G == 3) {
     round_g<T, 2, false>(v, tw, xt, p, c);
-    regroup<T, 2, 1>(v, sm, xt, tid);
+    regroup<T, 2, 1>(v, x.sm1, xt, tid, x.wait1);
     round_g<T, 1, false>(v, tw, xt, p, c);
-    regroup<T, 1, 0>(v, sm, xt, tid);
+    regroup<T, 1, 0>(v, x.sm2, xt, tid, x.wait2);
     round_g<T, 0, false>(v, tw, xt, p, c);
   } else if constexpr (G == 2) {
     round_g<T, 1, false>(v, tw, xt, p, c);
-    regroup<T, 1, 0>(v, sm, xt, tid);
+    regroup<T, 1, 0>(v, x.sm1, xt, tid, x.wait1);
     round_g<T, 0, false>(v, tw, xt, p, c);
   } else {
     round_g<T, 0, false>(v, tw, xt, p, c);
@@ -211,16 +223,16 @@ __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], uint64_t *sm, 
 // All inverse rounds, from group 0 up to the top group.  CANON_IN: the
 // residues come from the pointwise product, in [0, p).
 template <int T, bool CANON_IN = false>
-__device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], uint64_t *sm, const ulonglong2 *tw, uint32_t &xt,
+__device__ __forceinline__ void inverse_rounds(uint64_t (&v)[16], Exchanges x, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
   round_g<T, 0, true, CANON_IN>(v, tw, xt, p, c);
   if constexpr (G >= 2) {
-    regroup<T, 0, 1>(v, sm, xt, tid);
+    regroup<T, 0, 1>(v, x.sm1, xt, tid, x.wait1);
     round_g<T, 1, true>(v, tw, xt, p, c);
   }
   if constexpr (G == 3) {
-    regroup<T, 1, 2>(v, sm, xt, tid);
+    regroup<T, 1, 2>(v, x.sm2, xt, tid, x.wait2);
     round_g<T, 2, true>(v, tw, xt, p, c);
   }
 }
