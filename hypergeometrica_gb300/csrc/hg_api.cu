@@ -451,15 +451,15 @@ double pass_bytes(const PassArgs &a, int readers, int writers) {
 // them (one Montgomery product per residue).  Larger passes form them.
 constexpr int kPassTwiddleMaxLogM = 25;
 std::mutex g_ptw_mu;
-std::map<std::tuple<int, int, bool>, DevBuf> g_ptw;
+std::map<std::tuple<int, int, bool, bool>, DevBuf> g_ptw;
 
 // A table not built yet is not built while `st` is being captured into a
 // CUDA graph (that would allocate and synchronise inside the capture): the
 // pass then forms its twiddles.
-const uint64_t *pass_twiddles(int logM, int logR, bool inverse, cudaStream_t st) {
+const uint64_t *pass_twiddles(int logM, int logR, bool inverse, cudaStream_t st, const uint64_t *scale = nullptr) {
   if (logM > kPassTwiddleMaxLogM) return nullptr;
   std::lock_guard<std::mutex> lk(g_ptw_mu);
-  const auto key = std::make_tuple(logM, logR, inverse);
+  const auto key = std::make_tuple(logM, logR, inverse, scale != nullptr);
   auto it = g_ptw.find(key);
   if (it != g_ptw.end()) return it->second.u64();
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -475,7 +475,7 @@ const uint64_t *pass_twiddles(int logM, int logR, bool inverse, cudaStream_t st)
   }
   cudaStream_t bs = nullptr;
   if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess ||
-      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, bs) != cudaSuccess ||
+      launch_pass_twiddles(b.u64(), logM, logR, inverse, g_ctx.tb, g_ctx.pc, kPrimes, bs, scale) != cudaSuccess ||
       cudaStreamSynchronize(bs) != cudaSuccess) {
     if (bs) cudaStreamDestroy(bs);
     cudaGetLastError();
@@ -495,9 +495,12 @@ void release_pass_twiddles() {
 }
 
 // Strided passes [s0, s1) of `plan` (whose last entry is the contiguous
-// pass), forward in order or inverse in reverse order.
+// pass), forward in order or inverse in reverse order.  scale_last (inverse
+// only): the last inverse pass reads its table multiplied by these
+// Montgomery-form factors, and *scaled says whether it did (it forms its
+// twiddles unscaled when no table can be had).
 cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, bool inverse, int s0, int s1,
-                              cudaStream_t st) {
+                              cudaStream_t st, const uint64_t *scale_last = nullptr, bool *scaled = nullptr) {
   const int np = static_cast<int>(plan.size()) - 1;
   for (int s = s0; s < s1 && s < np; ++s) {
     const PassPlan &pp = plan[inverse ? np - 1 - s : s];
@@ -505,7 +508,9 @@ cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, boo
     a.logS = pp.logS;
     a.logT = pp.logT;
     a.tiles = (uint64_t(1) << a.logN) >> pp.logT;
-    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse, st);
+    const bool last_inverse = inverse && s == np - 1;
+    a.ptw = pass_twiddles(pp.logR + pp.logS, pp.logR, inverse, st, last_inverse ? scale_last : nullptr);
+    if (last_inverse && scaled) *scaled = scale_last && a.ptw;
     cudaError_t e;
     {
       ProfScope ps(inverse ? HG_KC_NTT_INVERSE : HG_KC_NTT_FORWARD, st, pass_bytes(a, a.nops, a.nops));
@@ -519,8 +524,9 @@ cudaError_t run_strided_range(PassArgs a, const std::vector<PassPlan> &plan, boo
 }
 
 // All strided passes of `plan`.
-cudaError_t run_strided(const PassArgs &a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st) {
-  return run_strided_range(a, plan, inverse, 0, static_cast<int>(plan.size()) - 1, st);
+cudaError_t run_strided(const PassArgs &a, const std::vector<PassPlan> &plan, bool inverse, cudaStream_t st,
+                        const uint64_t *scale_last = nullptr, bool *scaled = nullptr) {
+  return run_strided_range(a, plan, inverse, 0, static_cast<int>(plan.size()) - 1, st, scale_last, scaled);
 }
 
 // The contiguous pass (the plan's last entry) in the given mode.
@@ -535,8 +541,25 @@ cudaError_t run_contig(PassArgs a, const PassPlan &pp, int mode, cudaStream_t st
   return launch_ntt_contig(a, mode, st);
 }
 
-CrtConst crt_const(int L) {
+// Montgomery-form factors N^-1 2^64 mod p_j for a 2^L-point product, which a
+// product's last inverse pass folds into its table so that the
+// reconstruction receives the coefficients mod p_j; false where the moduli
+// do not meet the prescaled reconstruction's bounds (p0 < 2 p1, p0 < 2 p2,
+// 3 p2 < 2^64).
+bool prescale_factors(int L, uint64_t (&s)[kPrimes]) {
+  const uint64_t p0 = g_ctx.moduli[0], p1 = g_ctx.moduli[1], p2 = g_ctx.moduli[2];
+  if (!(p0 < 2 * p1 && p0 < 2 * p2 && p2 < ~uint64_t(0) / 3)) return false;
+  const uint64_t N = uint64_t(1) << L;
+  for (int j = 0; j < kPrimes; ++j) {
+    const uint64_t p = g_ctx.moduli[j];
+    s[j] = mont_h(mulmod_h(invmod_h(N % p, p), mont_h(1, p), p), p);
+  }
+  return true;
+}
+
+CrtConst crt_const(int L, bool prescaled = false) {
   CrtConst k{};
+  k.prescaled = prescaled ? 1u : 0u;
   const uint64_t p0 = g_ctx.moduli[0], p1 = g_ctx.moduli[1], p2 = g_ctx.moduli[2];
   for (int i = 0; i < kPrimes; ++i) k.pc[i] = g_ctx.pc[i];
   const uint64_t N = uint64_t(1) << L;
@@ -551,6 +574,7 @@ CrtConst crt_const(int L) {
   k.k2a = pair(mulmod_h(mulmod_h(n2, R2, p2), inv012, p2), p2);
   k.k2b = pair(inv012, p2);
   k.k2c = pair(mulmod_h(p0 % p2, inv012, p2), p2);
+  k.kp0 = pair(p0 % p2, p2);
   const u128 p01 = (u128)p0 * p1;
   k.p01_lo = static_cast<uint64_t>(p01);
   k.p01_hi = static_cast<uint64_t>(p01 >> 64);
@@ -861,7 +885,9 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   }
   PassArgs inv = base_args(L, 1);
   inv.data[0] = c.lane->A.u64();
-  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
+  uint64_t sc[kPrimes];
+  bool scaled = false;
+  HG_CUDA(run_strided(inv, plan, true, st, prescale_factors(L, sc) ? sc : nullptr, &scaled), "inverse transform");
   if (nout > N) HG_CUDA(cudaMemsetAsync(out + N, 0, (nout - N) * sizeof(uint64_t), st), "zero tail");
   ScanState ss;
   const uint64_t nproc = nout < N ? nout : N;
@@ -870,7 +896,8 @@ int ntt_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint64
   uint64_t tiles = 0;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(nproc), 2);  // local scan + fix
-    HG_CUDA(launch_crt_carry(c.lane->A.u64(), L, crt_const(L), out, nout, ss, st, &tiles), "reconstruction");
+    HG_CUDA(launch_crt_carry(c.lane->A.u64(), L, crt_const(L, scaled), out, nout, ss, st, &tiles),
+            "reconstruction");
   }
   HG_CUDA(ws_release(st), "workspace ordering");
   return HG_OK;

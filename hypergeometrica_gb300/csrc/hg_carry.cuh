@@ -39,8 +39,9 @@ __device__ __forceinline__ void add128_to(V3 &acc, uint64_t lo, uint64_t hi) {
 // COHERENT: the residues were written earlier in the same launch (the
 // persistent batch kernel), so they are read through L2 (ld.global.cg)
 // rather than the read-only data path, which is coherent only for data no
-// CTA of the launch writes.
-template <bool COHERENT = false>
+// CTA of the launch writes.  PRESCALED: the residues are the coefficients
+// mod p_j (CrtConst::prescaled).
+template <bool COHERENT = false, bool PRESCALED = false>
 struct CrtProducerT {
   const uint64_t *res;  // [3][N] natural-order residues from the unscaled inverse
   uint64_t n;           // N
@@ -83,20 +84,31 @@ struct CrtProducerT {
 
   __host__ __device__ __forceinline__ bool drop_top() const { return false; }
 
-  // Residues may be any 64-bit values congruent to the coefficient (the
-  // inverse leaves [0, 2p)): every one enters through a Shoup product.
+  // Residues lie in [0, 2p) (the inverse leaves them there).  Unscaled,
+  // every one enters through a Shoup product that also applies N^-1 2^64.
+  // Prescaled (the residues are the coefficient mod p_j), Garner's steps
+  // need three Shoup products instead of six: y0 = c mod p0 is r0 folded,
+  // t1 = (c - y0) / p0 mod p1 takes (r1 - y0) reduced to (0, 2 p1), and
+  // t2 takes r2 - y0 + p2 in (0, 3 p2) as it is.  The host prescales only
+  // where p0 < 2 p1, p0 < 2 p2 and 3 p2 < 2^64 (the reference's moduli).
   __device__ __forceinline__ V3 garner(uint64_t r0, uint64_t r1, uint64_t r2) const {
     const uint64_t p0 = k.pc[0].p, p1 = k.pc[1].p, p2 = k.pc[2].p;
     const uint32_t c0 = k.pc[0].c, c1 = k.pc[1].c, c2 = k.pc[2].c;
     check_below(r0, 2 * p0);  // inverse residues live in [0, 2p)
     check_below(r1, 2 * p1);
     check_below(r2, 2 * p2);
-    const uint64_t y0 = shoup_mul(r0, k.k0.x, k.k0.y, p0, c0);
-    const uint64_t t1 =
-        sub_mod_borrow(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);
-    uint64_t t2 =
-        sub_mod_borrow(shoup_mul(r2, k.k2a.x, k.k2a.y, p2, c2), shoup_mul(y0, k.k2b.x, k.k2b.y, p2, c2), p2);
-    t2 = sub_mod_borrow(t2, shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
+    uint64_t y0, t1, t2;
+    if constexpr (PRESCALED) {
+      y0 = fold_p(r0, p0);
+      t1 = shoup_mul(fold_p(r1, p1) - fold_p(y0, p1) + p1, k.k1b.x, k.k1b.y, p1, c1);
+      t2 = sub_mod_borrow(shoup_mul(r2 - fold_p(y0, p2) + p2, k.k2b.x, k.k2b.y, p2, c2),
+                          shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
+    } else {
+      y0 = shoup_mul(r0, k.k0.x, k.k0.y, p0, c0);
+      t1 = sub_mod_borrow(shoup_mul(r1, k.k1a.x, k.k1a.y, p1, c1), shoup_mul(y0, k.k1b.x, k.k1b.y, p1, c1), p1);
+      t2 = sub_mod_borrow(shoup_mul(r2, k.k2a.x, k.k2a.y, p2, c2), shoup_mul(y0, k.k2b.x, k.k2b.y, p2, c2), p2);
+      t2 = sub_mod_borrow(t2, shoup_mul(t1, k.k2c.x, k.k2c.y, p2, c2), p2);
+    }
     // V = y0 + p0 t1 + (p0 p1) t2 < p0 p1 p2 < 2^188
     V3 v{y0, 0, 0};
     add128_to(v, p0 * t1, __umul64hi(p0, t1));

@@ -276,6 +276,7 @@ cudaError_t launch_crt_carry(const uint64_t *res, int logN, const CrtConst &cc, 
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
+  if (cc.prescaled) return launch_carry(carry::CrtProducerT<false, true>{res, n, cc}, out, nproc, tiles, ss, st);
   return launch_carry(CrtProducer{res, n, cc}, out, nproc, tiles, ss, st);
 }
 
@@ -285,7 +286,7 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
   const uint64_t tpp = carry_tiles(n);
   const uint64_t tiles = tpp * nprod;
   if (tiles == 0) return cudaSuccess;
-  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  if (tiles > 0x7fffffffull || cc.prescaled) return cudaErrorInvalidValue;
   return launch_carry(CrtProducer{res, n, cc}, nullptr, 0, tiles, ss, st, batch, tpp, ws_stride, n);
 }
 
@@ -293,7 +294,7 @@ cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int
                                     uint64_t nchunks, const CrtConst &cc, uint64_t *out, uint64_t nproc,
                                     const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
   const uint64_t n = 1ull << logN;
-  if (chunk % 8 || 2 * chunk < n || chunk > n || ws_stride % 2) return cudaErrorInvalidValue;
+  if (chunk % 8 || 2 * chunk < n || chunk > n || ws_stride % 2 || cc.prescaled) return cudaErrorInvalidValue;
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;

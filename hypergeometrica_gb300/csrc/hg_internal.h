@@ -120,13 +120,20 @@ __host__ __device__ __forceinline__ const uint64_t *pass_limbs(const PassArgs &P
 }
 
 // Constants of the Garner reconstruction for one transform length.
-// Each constant is a (value, Shoup companion) pair.
+// Each constant is a (value, Shoup companion) pair.  The residues are
+// N c 2^-64 mod p_j for the coefficient c (the inverse transform is
+// unscaled, the pointwise product Montgomery), unless `prescaled`: then the
+// product's last inverse pass read an inter-pass table multiplied by
+// N^-1 2^64 mod p_j, and the residues are c mod p_j (in [0, 2p_j)).
 struct CrtConst {
   PrimeConst pc[kPrimes];
   ulonglong2 k0;            // N^-1 2^64                                         mod p0
   ulonglong2 k1a, k1b;      // N^-1 2^64 p0^-1, p0^-1                            mod p1
   ulonglong2 k2a, k2b, k2c; // N^-1 2^64 (p0p1)^-1, (p0p1)^-1, p1^-1            mod p2
+  ulonglong2 kp0;           // p0                                                mod p2
   uint64_t p01_lo, p01_hi;  // p0 * p1
+  uint32_t prescaled;
+  uint32_t pad;
 };
 
 // Carry launch state: tile tickets and the tiles' published aggregates.
@@ -178,7 +185,7 @@ cudaError_t launch_scale(uint64_t *a, uint64_t n, uint64_t mont_factor, PrimeCon
 // Fill out[j * M + r * S + s] = w_M^(+-s * bitrev_R(r)) (Montgomery form) for
 // the primes j = 0 .. nprimes - 1 of tb, M = 2^logM, R = 2^logR, S = M / R.
 cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse, const NttTables *tb,
-                                 const PrimeConst *pc, int nprimes, cudaStream_t st);
+                                 const PrimeConst *pc, int nprimes, cudaStream_t st, const uint64_t *scale = nullptr);
 
 // Tiles a carry-scan launch over n positions uses.
 uint64_t carry_tiles(uint64_t n);

@@ -240,19 +240,25 @@ __global__ void __launch_bounds__(kTileThreads, 4)
   }
 }
 
+// The inter-pass twiddles w_M^(s * bitrev(r)) of one (M, R, direction) in
+// Montgomery form, [prime][r][s]; with scale[j] != 0 (a Montgomery-form
+// factor) every entry of prime j is multiplied by it.
 __global__ void pass_twiddles_kernel(uint64_t *out, int logM, int logR, bool inverse, NttTables t0, NttTables t1,
-                                     NttTables t2, PrimeConst c0, PrimeConst c1, PrimeConst c2) {
+                                     NttTables t2, PrimeConst c0, PrimeConst c1, PrimeConst c2, uint64_t s0,
+                                     uint64_t s1, uint64_t s2) {
   const uint64_t M = uint64_t(1) << logM;
   const int j = static_cast<int>(blockIdx.y);
   const NttTables &t = j == 0 ? t0 : (j == 1 ? t1 : t2);
   const PrimeConst &pc = j == 0 ? c0 : (j == 1 ? c1 : c2);
+  const uint64_t scale = j == 0 ? s0 : (j == 1 ? s1 : s2);
   const int logS = logM - logR;
   for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < M;
        e += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const uint64_t r = e >> logS, s = e & ((uint64_t(1) << logS) - 1);
     const uint64_t E = (s * bitrev(static_cast<uint32_t>(r), logR)) & (M - 1);
-    out[static_cast<uint64_t>(j) * M + e] =
-        table_twiddle(E, logM, inverse ? t.hi_inv : t.hi_fwd, inverse ? t.lo_inv : t.lo_fwd, pc.p, pc.c);
+    uint64_t w = table_twiddle(E, logM, inverse ? t.hi_inv : t.hi_fwd, inverse ? t.lo_inv : t.lo_fwd, pc.p, pc.c);
+    if (scale) w = mont_mul(w, scale, pc.p, pc.c);
+    out[static_cast<uint64_t>(j) * M + e] = w;
   }
 }
 
@@ -392,14 +398,15 @@ HG_CHECKED_READER(checked_fault_strided)
 #endif
 
 cudaError_t launch_pass_twiddles(uint64_t *out, int logM, int logR, bool inverse, const NttTables *tb,
-                                 const PrimeConst *pc, int nprimes, cudaStream_t st) {
+                                 const PrimeConst *pc, int nprimes, cudaStream_t st, const uint64_t *scale) {
   if (nprimes < 1 || nprimes > kPrimes || logR < 1 || logR > 8 || logM <= logR || logM > kLogNmax)
     return cudaErrorInvalidValue;
   const uint64_t M = uint64_t(1) << logM;
   const unsigned gx = static_cast<unsigned>(std::min<uint64_t>((M + 255) / 256, 152 * 64));
+  const int j1 = nprimes > 1 ? 1 : 0, j2 = nprimes > 2 ? 2 : 0;
   pass_twiddles_kernel<<<dim3(gx, static_cast<unsigned>(nprimes)), 256, 0, st>>>(
-      out, logM, logR, inverse, tb[0], tb[nprimes > 1 ? 1 : 0], tb[nprimes > 2 ? 2 : 0], pc[0],
-      pc[nprimes > 1 ? 1 : 0], pc[nprimes > 2 ? 2 : 0]);
+      out, logM, logR, inverse, tb[0], tb[j1], tb[j2], pc[0], pc[j1], pc[j2], scale ? scale[0] : 0,
+      scale ? scale[j1] : 0, scale ? scale[j2] : 0);
   return cudaGetLastError();
 }
 
