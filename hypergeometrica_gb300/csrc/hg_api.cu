@@ -724,7 +724,9 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   inv.data[0] = c.lane->A.u64();
   inv.nprod = cp.nchunks;
   inv.ws_stride = slab;
-  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
+  uint64_t sc[kPrimes];
+  bool scaled = false;
+  HG_CUDA(run_strided(inv, plan, true, st, prescale_factors(L, sc) ? sc : nullptr, &scaled), "inverse transform");
   const uint64_t size = nx + ny;
   if (nout > size) HG_CUDA(cudaMemsetAsync(out + size, 0, (nout - size) * sizeof(uint64_t), st), "zero tail");
   ScanState ss;
@@ -733,8 +735,8 @@ int chunk_product_device(const uint64_t *x, uint64_t nx, const uint64_t *y, uint
   uint64_t tiles = 0;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(size), 2);  // local scan + fix
-    HG_CUDA(launch_crt_carry_chunks(c.lane->A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L), out, size, ss, st,
-                                    &tiles),
+    HG_CUDA(launch_crt_carry_chunks(c.lane->A.u64(), slab, L, cp.chunk, cp.nchunks, crt_const(L, scaled), out, size,
+                                    ss, st, &tiles),
             "reconstruction");
   }
   HG_CUDA(ws_release(st), "workspace ordering");
@@ -1373,7 +1375,9 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   inv.nprod = g.nprod;
   inv.ws_stride = slab;
   inv.data[0] = ws;
-  HG_CUDA(run_strided(inv, plan, true, st), "inverse transform");
+  uint64_t sc[kPrimes];
+  bool scaled = false;
+  HG_CUDA(run_strided(inv, plan, true, st, prescale_factors(g.L, sc) ? sc : nullptr, &scaled), "inverse transform");
   ScanState ss;
   ss.ticket = bb.tickets + gi;
   ss.ticket_base = 0;
@@ -1382,7 +1386,7 @@ int run_group(const BatchGroup &g, size_t gi, const BatchBufs &bb, const std::ve
   ss.err = bb.err;
   {
     ProfScope ps(HG_KC_CARRY, st, 32.0 * static_cast<double>(N) * static_cast<double>(g.nprod), 2);  // tiles + fix
-    HG_CUDA(launch_crt_carry_batch(ws, slab, g.L, crt_const(g.L), d, g.nprod, ss, st), "reconstruction");
+    HG_CUDA(launch_crt_carry_batch(ws, slab, g.L, crt_const(g.L, scaled), d, g.nprod, ss, st), "reconstruction");
   }
   return HG_OK;
 }

@@ -38,8 +38,9 @@ constexpr int kCarryTile = kCarryThreads * kCarryPer;
 // summed residues is the exact sum.  The inverse leaves residues in
 // [0, 2p); each is folded to [0, p) before the sum, and Garner's Shoup
 // products take the sum in [0, 2p) as it is.
-struct ChunkProducer {
-  CrtProducer crt;      // res = chunk 0's residues, n = 2^logN
+template <class Crt>
+struct ChunkProducerT {
+  Crt crt;              // res = chunk 0's residues, n = 2^logN
   uint64_t stride;      // words between consecutive chunks' residues
   uint64_t chunk, nchunks;
 
@@ -286,7 +287,10 @@ cudaError_t launch_crt_carry_batch(const uint64_t *res, uint64_t ws_stride, int 
   const uint64_t tpp = carry_tiles(n);
   const uint64_t tiles = tpp * nprod;
   if (tiles == 0) return cudaSuccess;
-  if (tiles > 0x7fffffffull || cc.prescaled) return cudaErrorInvalidValue;
+  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+  if (cc.prescaled)
+    return launch_carry(carry::CrtProducerT<false, true>{res, n, cc}, nullptr, 0, tiles, ss, st, batch, tpp, ws_stride,
+                        n);
   return launch_carry(CrtProducer{res, n, cc}, nullptr, 0, tiles, ss, st, batch, tpp, ws_stride, n);
 }
 
@@ -294,13 +298,16 @@ cudaError_t launch_crt_carry_chunks(const uint64_t *res, uint64_t ws_stride, int
                                     uint64_t nchunks, const CrtConst &cc, uint64_t *out, uint64_t nproc,
                                     const ScanState &ss, cudaStream_t st, uint64_t *tiles_used) {
   const uint64_t n = 1ull << logN;
-  if (chunk % 8 || 2 * chunk < n || chunk > n || ws_stride % 2 || cc.prescaled) return cudaErrorInvalidValue;
+  if (chunk % 8 || 2 * chunk < n || chunk > n || ws_stride % 2) return cudaErrorInvalidValue;
   const uint64_t tiles = carry_tiles(nproc);
   *tiles_used = tiles;
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  return launch_carry(ChunkProducer{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks}, out, nproc, tiles, ss,
-                            st);
+  if (cc.prescaled)
+    return launch_carry(ChunkProducerT<carry::CrtProducerT<false, true>>{{res, n, cc}, ws_stride, chunk, nchunks}, out,
+                        nproc, tiles, ss, st);
+  return launch_carry(ChunkProducerT<CrtProducer>{CrtProducer{res, n, cc}, ws_stride, chunk, nchunks}, out, nproc,
+                      tiles, ss, st);
 }
 
 cudaError_t launch_large_sum(const uint64_t *a, uint64_t na, int64_t sa, const uint64_t *b, uint64_t nb, int64_t sb,
