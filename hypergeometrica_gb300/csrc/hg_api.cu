@@ -1488,6 +1488,9 @@ std::vector<PersistPhase> group_phases(const BatchGroup &g, const BatchBufs &bb,
   inv.nprod = g.nprod;
   inv.ws_stride = slab;
   inv.data[0] = ws;
+  uint64_t sc[kPrimes];
+  const bool can_scale = prescale_factors(g.L, sc);
+  bool scaled = false;
   for (int s = 0; s < np; ++s) {
     const PassPlan &pp = plan[np - 1 - s];
     PassArgs f = inv;
@@ -1495,7 +1498,9 @@ std::vector<PersistPhase> group_phases(const BatchGroup &g, const BatchBufs &bb,
     f.logS = pp.logS;
     f.logT = pp.logT;
     f.tiles = N >> pp.logT;
-    f.ptw = pass_twiddles(f.logR + f.logS, f.logR, true, st);
+    const bool last = s == np - 1;  // the last inverse pass: its table prescaled
+    f.ptw = pass_twiddles(f.logR + f.logS, f.logR, true, st, last && can_scale ? sc : nullptr);
+    if (last) scaled = can_scale && f.ptw;
     PersistPhase p = phase(kPhaseStrided, f.logR | 16, f.tiles * g.nprod * kPrimes);
     p.a = f;
     v.push_back(p);
@@ -1504,7 +1509,7 @@ std::vector<PersistPhase> group_phases(const BatchGroup &g, const BatchBufs &bb,
   c.res = ws;
   c.n = N;
   c.ws_stride = slab;
-  c.cc = crt_const(g.L);
+  c.cc = crt_const(g.L, scaled);
   c.batch = d;
   c.tpp = persist_carry_tiles(N);
   c.tiles = c.tpp * g.nprod;

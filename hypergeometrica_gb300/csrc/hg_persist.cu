@@ -83,10 +83,21 @@ __device__ __noinline__ void run_tiny(const PersistPhase &ph, uint64_t item) {
     tiny_body(ph.a, ph.sel, pair / ph.a.nprimes, static_cast<int>(pair % ph.a.nprimes));
 }
 
-__device__ __noinline__ void run_carry(const PersistPhase &ph, uint64_t item, uint64_t *dyn, GP *s_warp) {
-  carry::carry_body<carry::CrtProducerT<true>, kPersistThreads>(carry::CrtProducerT<true>{ph.res, ph.n, ph.cc}, nullptr, 0, ph.ss,
-                                                         ph.batch, ph.tpp, ph.ws_stride, ph.n, item,
-                                                         reinterpret_cast<uint64_t(*)[9]>(dyn), s_warp);
+// Residues prescaled (the group's last inverse pass read its scaled table)
+// or not: each reconstruction has its own body.
+template <bool PRESCALED>
+__device__ __noinline__ void run_carry_t(const PersistPhase &ph, uint64_t item, uint64_t *dyn, GP *s_warp) {
+  using Producer = carry::CrtProducerT<true, PRESCALED>;
+  carry::carry_body<Producer, kPersistThreads>(Producer{ph.res, ph.n, ph.cc}, nullptr, 0, ph.ss, ph.batch, ph.tpp,
+                                               ph.ws_stride, ph.n, item, reinterpret_cast<uint64_t(*)[9]>(dyn),
+                                               s_warp);
+}
+
+__device__ __forceinline__ void run_carry(const PersistPhase &ph, uint64_t item, uint64_t *dyn, GP *s_warp) {
+  if (ph.cc.prescaled)
+    run_carry_t<true>(ph, item, dyn, s_warp);
+  else
+    run_carry_t<false>(ph, item, dyn, s_warp);
 }
 
 __device__ __noinline__ void run_fix(const PersistPhase &ph, uint64_t item) {
