@@ -576,7 +576,6 @@ CrtConst crt_const(int L, bool prescaled = false) {
   k.k2a = pair(mulmod_h(mulmod_h(n2, R2, p2), inv012, p2), p2);
   k.k2b = pair(inv012, p2);
   k.k2c = pair(mulmod_h(p0 % p2, inv012, p2), p2);
-  k.kp0 = pair(p0 % p2, p2);
   const u128 p01 = (u128)p0 * p1;
   k.p01_lo = static_cast<uint64_t>(p01);
   k.p01_hi = static_cast<uint64_t>(p01 >> 64);

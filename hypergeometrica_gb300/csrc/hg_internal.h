@@ -130,7 +130,6 @@ struct CrtConst {
   ulonglong2 k0;            // N^-1 2^64                                         mod p0
   ulonglong2 k1a, k1b;      // N^-1 2^64 p0^-1, p0^-1                            mod p1
   ulonglong2 k2a, k2b, k2c; // N^-1 2^64 (p0p1)^-1, (p0p1)^-1, p1^-1            mod p2
-  ulonglong2 kp0;           // p0                                                mod p2
   uint64_t p01_lo, p01_hi;  // p0 * p1
   uint32_t prescaled;
   uint32_t pad;
