@@ -186,16 +186,17 @@ __device__ __forceinline__ uint64_t sub_mod_borrow(uint64_t a, uint64_t b, uint6
 
 __device__ __forceinline__ uint64_t mul_hi64(uint64_t a, uint64_t b) { return __umul64hi(a, b); }
 
-// Montgomery product a * b * 2^-64 mod p, for any 64-bit a and b < p, with
-// p = c * 2^55 + 1.  Result is fully reduced in [0, p).
+// Montgomery product a * b * 2^-64 mod p, for any 64-bit a and b < p (WIDE:
+// a, b < 2p), with p = c * 2^55 + 1.  Result is fully reduced in [0, p).
 //   m = lo * p^-1 mod 2^64 = lo - ((lo * c) mod 2^9) * 2^55   (m1:m0 below)
 //   floor(m * p / 2^64) = u * 2^23 + floor((t mod 2^32) / 2^9) with
 //   t = m0 * c + floor(m / 2^55) and u = m1 * c + floor(t / 2^32) < 2^40;
 // the last product and sum are formed with IMAD (mad.wide.u32), which keeps
 // them off the integer ALU pipe that the butterflies' additions load.
+template <bool WIDE = false>
 __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p, uint32_t c) {
   const uint64_t lo = a * b;
-  const uint64_t hi = mul_hi64(a, b);  // < p because a < 2^64 and b < p
+  const uint64_t hi = mul_hi64(a, b);  // < p because a < 2^64 and b < p (WIDE: a, b < 2p)
   const uint32_t m0 = static_cast<uint32_t>(lo);
   const uint32_t m1 = static_cast<uint32_t>(lo >> 32) - m0 * (c << 23);
   uint64_t t;
@@ -214,13 +215,23 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
       : "=l"(mph)
       : "r"(static_cast<uint32_t>(t)), "r"(static_cast<uint32_t>(u)));
   mph += static_cast<uint64_t>(static_cast<uint32_t>(u >> 32)) << 55;
-  const uint64_t r = hi >= mph ? hi - mph : hi - mph + p;  // low halves cancel exactly; hi, mph < p
+  uint64_t r;
+  if (WIDE)  // hi < (2p)^2 / 2^64 < 2p, so hi - mph lies in (-p, 2p)
+    r = hi >= mph ? fold_p(hi - mph, p) : hi - mph + p;
+  else
+    r = hi >= mph ? hi - mph : hi - mph + p;  // low halves cancel exactly; hi, mph < p
 #if HG_CHECKED
   // r 2^64 = a b (mod p), with 2^64 mod p = (2^32)^2 mod p
   if (r >= p || mulmod_exact(r, mulmod_exact(1ull << 32, 1ull << 32, p), p) != mulmod_exact(a, b, p))
     checked_fault(kDevProduct);
 #endif
   return r;
+}
+
+// The Montgomery product of a, b < 2p (both factors left uncorrected by the
+// last forward stage of the middle pass): one correction more.
+__device__ __forceinline__ uint64_t mont_mul_2p(uint64_t a, uint64_t b, uint64_t p, uint32_t c) {
+  return mont_mul<true>(a, b, p, c);
 }
 
 // Shoup product a * w mod p for any 64-bit a, w < p with companion

@@ -200,8 +200,10 @@ struct Exchanges {
 };
 __device__ __forceinline__ Exchanges through(uint64_t *sm) { return Exchanges{sm, sm, true, true}; }
 
-// All forward rounds, from the top group down to group 0.
-template <int T>
+// All forward rounds, from the top group down to group 0.  EDGE_LAST: the
+// last stage (twiddle 1) leaves its sums and differences uncorrected, in
+// [0, 2p), for a consumer that takes them (the pointwise mont_mul_2p).
+template <int T, bool EDGE_LAST = false>
 __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], Exchanges x, const ulonglong2 *tw, uint32_t &xt,
                                                uint32_t tid, uint64_t p, uint32_t c) {
   constexpr int G = Groups<T>::G;
@@ -210,13 +212,13 @@ __device__ __forceinline__ void forward_rounds(uint64_t (&v)[16], Exchanges x, c
     regroup<T, 2, 1>(v, x.sm1, xt, tid, x.wait1);
     round_g<T, 1, false>(v, tw, xt, p, c);
     regroup<T, 1, 0>(v, x.sm2, xt, tid, x.wait2);
-    round_g<T, 0, false>(v, tw, xt, p, c);
+    round_g<T, 0, false, EDGE_LAST>(v, tw, xt, p, c);
   } else if constexpr (G == 2) {
     round_g<T, 1, false>(v, tw, xt, p, c);
     regroup<T, 1, 0>(v, x.sm1, xt, tid, x.wait1);
-    round_g<T, 0, false>(v, tw, xt, p, c);
+    round_g<T, 0, false, EDGE_LAST>(v, tw, xt, p, c);
   } else {
-    round_g<T, 0, false>(v, tw, xt, p, c);
+    round_g<T, 0, false, EDGE_LAST>(v, tw, xt, p, c);
   }
 }
 
