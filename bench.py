@@ -649,7 +649,7 @@ def run_expt() -> dict:
 
 # Thread instructions per radix-2 butterfly of the middle kernel (ncu,
 # profiles/ntt_contig_mul_2e22.md): the fewest any pass of the product spends.
-INSTR_PER_BUTTERFLY = 29.4
+INSTR_PER_BUTTERFLY = 29.2
 
 
 def _int_roofline(N: int, ms_per_product: float, sm_mhz) -> dict:
@@ -658,7 +658,7 @@ def _int_roofline(N: int, ms_per_product: float, sm_mhz) -> dict:
     of the same modular butterflies over every SM measured now, and the
     issue-rate floor, every SM sub-partition issuing one warp instruction
     per clock at the clock sampled under load, with the middle kernel's
-    29.4 thread instructions per butterfly."""
+    29.2 thread instructions per butterfly."""
     import ctypes
 
     import torch
