@@ -216,7 +216,7 @@ __device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p,
       : "r"(static_cast<uint32_t>(t)), "r"(static_cast<uint32_t>(u)));
   mph += static_cast<uint64_t>(static_cast<uint32_t>(u >> 32)) << 55;
   uint64_t r;
-  if (WIDE)  // hi < (2p)^2 / 2^64 < 2p, so hi - mph lies in (-p, 2p)
+  if constexpr (WIDE)  // hi < (2p)^2 / 2^64 < 2p, so hi - mph lies in (-p, 2p)
     r = hi >= mph ? fold_p(hi - mph, p) : hi - mph + p;
   else
     r = hi >= mph ? hi - mph : hi - mph + p;  // low halves cancel exactly; hi, mph < p
